@@ -1,0 +1,204 @@
+/*
+ * les_gpu.h -- C-ABI of the GB300 (sm_103a) per-timestep solver of MPI-LES.
+ *
+ * The library keeps one urban domain (or a batch of domains) resident in GPU memory
+ * and advances it with the reference's eight solver subroutines, in the step order
+ * of src/main.f95:260-296 (velnw -> bondv1 -> velfg -> feedbf -> les -> adam -> press).
+ * Each entry point below replaces one reference interface; the replaced Fortran
+ * routine is cited beside it.  Plain C types only: no CUDA or torch types cross
+ * this boundary, so Fortran (ISO_C_BINDING), C, C++ and Python (ctypes) can bind it.
+ *
+ * Conventions
+ *   - Every function returns an int status: LES_OK (0) or a negative LES_ERR_* code.
+ *     les_gpu_last_error() gives the message of the last failure on a handle.
+ *   - Arrays cross the boundary in the reference's Fortran layout: column-major,
+ *     i fastest, with the declared lower/upper bounds passed as lb[3]/ub[3]
+ *     (for example u is (0:im+1,-1:jm+1,0:km+1), src/main.f95:147).  1-D arrays use
+ *     lb[0]/ub[0] with lb[1]=ub[1]=lb[2]=ub[2]=0; 2-D arrays use lb[0..1]/ub[0..1].
+ *   - Work is queued on the handle's own CUDA stream.  Calls on one handle must come
+ *     from one host thread at a time.  les_gpu_download() and les_gpu_sync() are the
+ *     synchronisation points (like the reads of src/module_LES_combined_ocl.f95:562-571).
+ *   - There is no CPU fallback: without a usable GPU, les_gpu_create() fails with
+ *     LES_ERR_CUDA.
+ */
+#ifndef LES_GPU_H
+#define LES_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LES_GPU_ABI_VERSION 1
+
+/* status codes */
+#define LES_OK 0
+#define LES_ERR_ARG (-1)      /* bad argument (size, extents, field id, value)      */
+#define LES_ERR_CUDA (-2)     /* CUDA runtime error (message in last_error)         */
+#define LES_ERR_STATE (-3)    /* call out of order (e.g. step before setup commit)  */
+#define LES_ERR_NOMEM (-4)    /* device memory exhausted                            */
+#define LES_ERR_NUMERIC (-5)  /* non-finite values detected by les_gpu_check_finite */
+#define LES_ERR_BUSY (-6)     /* batch slot or request refused (capacity)           */
+
+/* Field ids.  3-D state and work arrays (extents as declared in src/main.f95:63-159). */
+enum les_field {
+  LES_FIELD_U = 1,      /* (0:im+1,-1:jm+1, 0:km+1)  main.f95:147 */
+  LES_FIELD_V = 2,      /* (0:im+1,-1:jm+1, 0:km+1)  main.f95:151 */
+  LES_FIELD_W = 3,      /* (0:im+1,-1:jm+1,-1:km+1)  main.f95:153 */
+  LES_FIELD_P = 4,      /* (0:im+2, 0:jm+2, 0:km+1)  main.f95:144 */
+  LES_FIELD_F = 5,      /* (0:im, 0:jm, 0:km)        main.f95:120 */
+  LES_FIELD_G = 6,
+  LES_FIELD_H = 7,
+  LES_FIELD_FOLD = 8,   /* (1:im, 1:jm, 1:km)        main.f95:124 */
+  LES_FIELD_GOLD = 9,
+  LES_FIELD_HOLD = 10,
+  LES_FIELD_USUM = 11,  /* (0:im, 0:jm, 0:km)        main.f95:148 */
+  LES_FIELD_VSUM = 12,
+  LES_FIELD_WSUM = 13,
+  LES_FIELD_RHS = 14,   /* (0:im+1, 0:jm+1, 0:km+1)  main.f95:145 */
+  LES_FIELD_SM = 15,    /* (-1:im+1,-1:jm+1, 0:km+1) main.f95:146 */
+  LES_FIELD_BMASK1 = 16,/* (-1:im+1, 0:jm+1, 0:km+1) upload only; values 0 or 1 */
+  LES_FIELD_CMASK1 = 17,/* (0:im+1,-1:jm+1, 0:km+1)  upload only; values 0 or 1 */
+  LES_FIELD_DMASK1 = 18,/* (0:im+1, 0:jm+1, 0:km+1)  upload only; values 0 or 1 */
+  LES_FIELD_CN1 = 20,   /* (1:im, 1:jm, 1:km)        upload only (init.f95:98-104) */
+  /* 1-D grid and Poisson coefficient arrays (grid.f95, init.f95:82-95) */
+  LES_FIELD_DX1 = 32,   /* (-1:im+1) */
+  LES_FIELD_DY1 = 33,   /* (0:jm+1)  */
+  LES_FIELD_DZN = 34,   /* (-1:km+2) */
+  LES_FIELD_DZS = 35,   /* (-1:km+2) */
+  LES_FIELD_DXS = 36,   /* (0:im)    */
+  LES_FIELD_DYS = 37,   /* (0:jm)    */
+  LES_FIELD_Z2 = 38,    /* (0:km+2)  */
+  LES_FIELD_CN2L = 39,  /* (1:im)    */
+  LES_FIELD_CN2S = 40,
+  LES_FIELD_CN3L = 41,  /* (1:jm)    */
+  LES_FIELD_CN3S = 42,
+  LES_FIELD_CN4L = 43,  /* (1:km)    */
+  LES_FIELD_CN4S = 44,
+  LES_FIELD_DELX1 = 45, /* (1:km) download only: les.f95:38-42 */
+  /* 2-D inflow planes applied by bondv1 on i = 0, 1 (replace bondv1.f95:33-54) */
+  LES_FIELD_UIN = 53,   /* (1:jm, 1:km) */
+  LES_FIELD_VIN = 54,
+  LES_FIELD_WIN = 55
+};
+
+typedef struct les_dims {
+  int im, jm, km;       /* interior cells; jm must be even for the fused SOR sweep */
+} les_dims;
+
+typedef struct les_params {
+  float dt, ro, vn;     /* set.f95:89-92 (0.05, 1.1763, 15.83e-6)                */
+  float alpha, beta;    /* IBM feedback gains, set.f95:94-95 (-10, -1)           */
+  float omega, pjuge;   /* SOR relaxation and tolerance, press.f95:43-45         */
+  int nmaxp;            /* SOR iteration cap, press.f95:44 (50)                  */
+  int sor_fixed;        /* 1: always nmaxp iterations; 0: exit on sor < pjuge     */
+  int sor_depth;        /* SOR iterations fused per pass: 0 = autotuned, 1..4     */
+} les_params;
+
+/* Synthetic urban scenario (the configs' generator; replaces the GIS inputs read
+ * by feedbfm.f95:52-77 and the fixed inflow of bondv1.f95:33-54). */
+typedef struct les_scenario {
+  int im, jm, km;
+  float dx, dy;                 /* 4 m, grid.f95:36-69                              */
+  int dz_law;                   /* 0: grid.f95:114-135 law; 1: geometric            */
+  float dz0, dz_ratio;          /* geometric law: dzn(1) = dz0, dzn(k) = dzn(k-1)*r  */
+  unsigned long long seed;
+  float coverage;               /* building plan-area fraction (0 = no buildings)    */
+  int fp_min, fp_max;           /* block footprint side, cells                       */
+  float h_min, h_max;           /* block height, m                                   */
+  int inflow_law;               /* 0: 5 m/s uniform (bondv1.f95:33-54); 1: power law */
+  float u_ref, z_ref, pl_exp;   /* power law U(z) = u_ref*(z/z_ref)^pl_exp           */
+  float direction_deg;          /* inflow direction, degrees                         */
+  float noise;                  /* fixed uniform +-noise on inflow cells, m/s        */
+} les_scenario;
+
+typedef struct les_handle les_handle;
+
+/* ---- host-side setup (run once per domain; no GPU needed) ---------------------- */
+
+/* grid.f95:5-182 for runtime sizes.  Output arrays at their Fortran extents:
+ * dx1(-1:im+1) dxl(0:im) dxs(0:im) dy1(0:jm+1) dyl(0:jm) dys(0:jm) dzn(-1:km+2)
+ * dzs(-1:km+2) z2(0:km+2). */
+int les_setup_grid(int im, int jm, int km, float dx, float dy, int dz_law, float dz0,
+                   float dz_ratio, float *dx1, float *dxl, float *dxs, float *dy1, float *dyl,
+                   float *dys, float *dzn, float *dzs, float *z2);
+/* init.f95:82-107: cn2s,cn2l(1:im) cn3s,cn3l(1:jm) cn4s,cn4l(1:km) cn1(1:im,1:jm,1:km);
+ * cn1 may be NULL. */
+int les_setup_poisson(int im, int jm, int km, const float *dxs, const float *dys,
+                      const float *dzs, float *cn2s, float *cn2l, float *cn3s, float *cn3l,
+                      float *cn4s, float *cn4l, float *cn1);
+/* feedbfm.f95:25-116 with zbm(1:im,1:jm) given: masks at their Fortran extents. */
+int les_setup_masks(int im, int jm, int km, const float *zbm, const float *z2,
+                    const float *dzn, float *amask1, float *bmask1, float *cmask1,
+                    float *dmask1);
+/* Seeded synthetic scenario: zbm(1:im,1:jm) heightmap and uin/vin/win(1:jm,1:km)
+ * inflow planes.  Deterministic for a given seed on every host. */
+int les_scenario_generate(const les_scenario *sc, float *zbm, float *uin, float *vin,
+                          float *win);
+/* Bytes of device memory one domain of this size needs (admission control). */
+size_t les_domain_bytes(int im, int jm, int km);
+
+/* ---- one resident domain ------------------------------------------------------- */
+
+/* Allocate the device state of one domain, all fields zero (init.f95:46-69).
+ * Replaces the buffer set-up of initialise_LES_kernel (module_LES_combined_ocl.f95:14). */
+int les_gpu_create(const les_dims *dims, const les_params *params, les_handle **out);
+int les_gpu_destroy(les_handle *h);
+/* Copy a field between host (Fortran layout, extents lb..ub) and device. */
+int les_gpu_upload(les_handle *h, int field, const float *host, const int lb[3],
+                   const int ub[3]);
+int les_gpu_download(les_handle *h, int field, float *host, const int lb[3],
+                     const int ub[3]);
+/* Validate the uploaded grid/coefficients/masks/inflow and derive the per-domain
+ * constants (les.f95:38-42 delx1, the log-law factor of vel2.f95:138).  Required
+ * once before the first solver call and after any later grid upload. */
+int les_gpu_commit_setup(les_handle *h);
+/* Convenience: generate the scenario, run the host setup and upload + commit. */
+int les_gpu_setup_scenario(les_handle *h, const les_scenario *sc);
+
+/* The eight solver subroutines, on device-resident state. */
+int les_gpu_velnw(les_handle *h);                    /* velnw.f95:5   */
+int les_gpu_bondv1(les_handle *h, int n);            /* bondv1.f95:5  */
+int les_gpu_velfg(les_handle *h);                    /* velFG.f95:6 (vel2 fused)   */
+int les_gpu_feedbf(les_handle *h);                   /* feedbf.f95:5  */
+int les_gpu_les(les_handle *h);                      /* les.f95:6 (boundsm fused)  */
+int les_gpu_adam(les_handle *h);                     /* adam.f95:5    */
+int les_gpu_press(les_handle *h, int n, int nmax);   /* press.f95:9   */
+int les_gpu_bondfg(les_handle *h);                   /* bondFG.f95:5  */
+int les_gpu_boundp1(les_handle *h);                  /* boundp.f95:28 */
+int les_gpu_boundp2(les_handle *h);                  /* boundp.f95:7  */
+
+/* One whole time step n (velnw .. press) through the fused kernels, launched as a
+ * captured CUDA graph.  Mirrors run_LES_kernel(n, nmax), main.f95:251. */
+int les_gpu_step(les_handle *h, int n, int nmax);
+/* Steps n0 .. n0+nsteps-1 back to back (the main.f95:247 loop body). */
+int les_gpu_run(les_handle *h, int n0, int nsteps, int nmax);
+int les_gpu_sync(les_handle *h);
+/* Diagnostics of the last press call: out[0] SOR iterations, out[1] last residual
+ * sum (FP64), out[2] uout, out[3] rhsav, out[4] pav.  Synchronises. */
+int les_gpu_diag(les_handle *h, double out[5]);
+/* Sets *bad to the number of non-finite interior values of u, v, w, p. */
+int les_gpu_check_finite(les_handle *h, long long *bad);
+/* The handle's CUDA stream (a cudaStream_t), for callers that time or overlap work. */
+int les_gpu_stream(les_handle *h, void **stream);
+/* Kernel launches issued on this handle since creation (all stages). */
+long long les_gpu_launch_count(les_handle *h);
+int les_gpu_last_error(les_handle *h, char *buf, size_t len);
+
+/* Profiling: queue `reps` back-to-back launches of one stage on the handle's stream,
+ * bracketed by CUDA events, and return the average milliseconds per repetition.
+ * The stage really runs (it advances the state).  what: LES_PROF_*. */
+enum les_prof {
+  LES_PROF_SOR = 0,    /* one SOR iteration of press, as the whole step runs it */
+  LES_PROF_VELFG = 1,  /* velfg (+ feedbf when fused in the step)                */
+  LES_PROF_LES = 2,    /* les: eddy viscosity and viscous terms (+ adam fused)   */
+  LES_PROF_VELNW = 3,
+  LES_PROF_STEP = 4    /* one whole step (n > 1)                                 */
+};
+int les_gpu_profile(les_handle *h, int what, int reps, double *ms_avg);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LES_GPU_H */

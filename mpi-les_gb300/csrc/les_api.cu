@@ -1,0 +1,639 @@
+// les_api.cu -- the C-ABI of include/les_gpu.h: one resident domain per handle.
+//
+// Replaces the reference's buffer set-up and per-step driver of the OpenCL path
+// (initialise_LES_kernel / run_LES_kernel, src/module_LES_combined_ocl.f95:14,350)
+// and, entry point by entry point, the eight Fortran solver subroutines.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/les_gpu.h"
+#include "les_common.cuh"
+#include "les_kernels.cuh"
+#include "les_step.cuh"
+
+namespace {
+
+constexpr int kNumFields = 15;  // LES_FIELD_U .. LES_FIELD_SM
+
+struct Ext {
+  int lb[3], ub[3];
+};
+
+// Declared extents of each field in the reference (src/main.f95:63-159).
+bool declared_extents(int id, int im, int jm, int km, Ext *e) {
+  auto set = [&](int a0, int b0, int a1, int b1, int a2, int b2) {
+    e->lb[0] = a0; e->ub[0] = b0; e->lb[1] = a1; e->ub[1] = b1; e->lb[2] = a2; e->ub[2] = b2;
+  };
+  switch (id) {
+    case LES_FIELD_U: case LES_FIELD_V: set(0, im + 1, -1, jm + 1, 0, km + 1); return true;
+    case LES_FIELD_W: set(0, im + 1, -1, jm + 1, -1, km + 1); return true;
+    case LES_FIELD_P: set(0, im + 2, 0, jm + 2, 0, km + 1); return true;
+    case LES_FIELD_F: case LES_FIELD_G: case LES_FIELD_H:
+    case LES_FIELD_USUM: case LES_FIELD_VSUM: case LES_FIELD_WSUM: set(0, im, 0, jm, 0, km); return true;
+    case LES_FIELD_FOLD: case LES_FIELD_GOLD: case LES_FIELD_HOLD: set(1, im, 1, jm, 1, km); return true;
+    case LES_FIELD_RHS: set(0, im + 1, 0, jm + 1, 0, km + 1); return true;
+    case LES_FIELD_SM: set(-1, im + 1, -1, jm + 1, 0, km + 1); return true;
+    case LES_FIELD_BMASK1: set(-1, im + 1, 0, jm + 1, 0, km + 1); return true;
+    case LES_FIELD_CMASK1: set(0, im + 1, -1, jm + 1, 0, km + 1); return true;
+    case LES_FIELD_DMASK1: set(0, im + 1, 0, jm + 1, 0, km + 1); return true;
+    case LES_FIELD_CN1: set(1, im, 1, jm, 1, km); return true;
+    case LES_FIELD_DX1: set(-1, im + 1, 0, 0, 0, 0); return true;
+    case LES_FIELD_DY1: set(0, jm + 1, 0, 0, 0, 0); return true;
+    case LES_FIELD_DZN: case LES_FIELD_DZS: set(-1, km + 2, 0, 0, 0, 0); return true;
+    case LES_FIELD_DXS: set(0, im, 0, 0, 0, 0); return true;
+    case LES_FIELD_DYS: set(0, jm, 0, 0, 0, 0); return true;
+    case LES_FIELD_Z2: set(0, km + 2, 0, 0, 0, 0); return true;
+    case LES_FIELD_CN2L: case LES_FIELD_CN2S: set(1, im, 0, 0, 0, 0); return true;
+    case LES_FIELD_CN3L: case LES_FIELD_CN3S: set(1, jm, 0, 0, 0, 0); return true;
+    case LES_FIELD_CN4L: case LES_FIELD_CN4S: case LES_FIELD_DELX1: set(1, km, 0, 0, 0, 0); return true;
+    case LES_FIELD_UIN: case LES_FIELD_VIN: case LES_FIELD_WIN: set(1, jm, 1, km, 0, 0); return true;
+    default: return false;
+  }
+}
+
+bool is_1d(int id) { return id >= LES_FIELD_DX1 && id <= LES_FIELD_DELX1; }
+bool is_inflow(int id) { return id >= LES_FIELD_UIN && id <= LES_FIELD_WIN; }
+
+}  // namespace
+
+struct les_handle {
+  les_dims dims{};
+  les_params prm{};
+  int pi = 0, nj = 0, np = 0;
+  size_t nfloat = 0;  // floats per padded 3-D field
+  int dev = 0;
+  cudaStream_t s = nullptr;
+  float *fields[kNumFields] = {};
+  uint8_t *mask_d = nullptr;
+  std::vector<uint8_t> mask_h;
+  bool mask_dirty = true;
+  std::map<int, std::vector<float>> h1d;  // 1-D arrays and inflow planes (host copies)
+  float *g1_d = nullptr;                  // 1-D arrays on the device
+  float *inflow_d = nullptr;
+  std::vector<float> cn1_h;
+  bool cn1_given = false;
+  float *cn1_d = nullptr;
+  double *scal_d = nullptr;
+  int *ctl_d = nullptr;
+  double *part_d = nullptr;
+  float *fscal_d = nullptr;
+  unsigned long long *bad_d = nullptr;
+  size_t npart = 0;
+  bool committed = false;
+  LesDom dom{};
+  long long nlaunch = 0;
+  std::string err;
+  LesStepPlan plan{};
+};
+
+namespace {
+
+int fail(les_handle *h, int code, const std::string &msg) {
+  if (h) h->err = msg;
+  return code;
+}
+
+int cuda_fail(les_handle *h, cudaError_t e, const char *what) {
+  std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+  (void)cudaGetLastError();
+  return fail(h, e == cudaErrorMemoryAllocation ? LES_ERR_NOMEM : LES_ERR_CUDA, m);
+}
+
+#define CK(h, call)                                   \
+  do {                                                \
+    cudaError_t e_ = (call);                          \
+    if (e_ != cudaSuccess) return cuda_fail(h, e_, #call); \
+  } while (0)
+
+int check_launch(les_handle *h, const char *what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(h, e, what);
+  return LES_OK;
+}
+
+LesCtx ctx_of(les_handle *h) { return LesCtx{h->s, &h->nlaunch}; }
+
+int pitch_for(int im) { return ((im + 6) + 15) / 16 * 16; }
+
+}  // namespace
+
+extern "C" size_t les_domain_bytes(int im, int jm, int km) {
+  const size_t pi = (size_t)pitch_for(im), nj = (size_t)jm + 4, nk = (size_t)km + 4;
+  const size_t field = pi * nj * nk * sizeof(float);
+  const size_t part = ((size_t)(im + 63) / 64 + 1) * ((size_t)(jm + 3) / 4 + 1) * (size_t)km * 2 * sizeof(double);
+  return kNumFields * field + pi * nj * nk /*mask bytes*/ + part + 64 * 1024;
+}
+
+extern "C" int les_gpu_create(const les_dims *dims, const les_params *params, les_handle **out) {
+  if (!dims || !params || !out) return LES_ERR_ARG;
+  *out = nullptr;
+  const int im = dims->im, jm = dims->jm, km = dims->km;
+  if (im < 3 || jm < 2 || km < 3) return LES_ERR_ARG;
+  if (params->nmaxp < 0 || params->nmaxp > 100000) return LES_ERR_ARG;
+  les_handle *h = new les_handle();
+  h->dims = *dims;
+  h->prm = *params;
+  h->pi = pitch_for(im);
+  h->nj = jm + 4;
+  h->np = h->pi * h->nj;
+  h->nfloat = (size_t)h->np * (size_t)(km + 4);
+  if (h->nfloat >= (size_t)1 << 31) {
+    delete h;
+    return LES_ERR_ARG;  // 32-bit indexing inside the kernels
+  }
+  auto cleanup = [&](int code) {
+    les_gpu_destroy(h);
+    return code;
+  };
+  cudaError_t e = cudaGetDevice(&h->dev);
+  if (e != cudaSuccess) { (void)cudaGetLastError(); return cleanup(LES_ERR_CUDA); }
+  if ((e = cudaStreamCreateWithFlags(&h->s, cudaStreamNonBlocking)) != cudaSuccess) { (void)cudaGetLastError(); return cleanup(LES_ERR_CUDA); }
+  for (int f = 0; f < kNumFields; ++f) {
+    if ((e = cudaMalloc(&h->fields[f], h->nfloat * sizeof(float))) != cudaSuccess) {
+      (void)cudaGetLastError();
+      return cleanup(LES_ERR_NOMEM);
+    }
+    if ((e = cudaMemsetAsync(h->fields[f], 0, h->nfloat * sizeof(float), h->s)) != cudaSuccess) {
+      (void)cudaGetLastError();
+      return cleanup(LES_ERR_CUDA);
+    }
+  }
+  if (cudaMalloc(&h->mask_d, h->nfloat) != cudaSuccess) { (void)cudaGetLastError(); return cleanup(LES_ERR_NOMEM); }
+  h->mask_h.assign(h->nfloat, 0);
+  // partial-sum buffer: the largest per-block count of any reduction kernel
+  h->npart = (size_t)std::max<long long>(
+      {(long long)((im + 63) / 64) * ((jm + 3) / 4) * km * 2 + 64, (long long)les_step_parts_needed(im, jm, km)});
+  if (cudaMalloc(&h->part_d, h->npart * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&h->scal_d, SC_COUNT * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&h->ctl_d, CT_COUNT * sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&h->fscal_d, SC_COUNT * sizeof(float)) != cudaSuccess ||
+      cudaMalloc(&h->bad_d, sizeof(unsigned long long)) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return cleanup(LES_ERR_NOMEM);
+  }
+  cudaMemsetAsync(h->scal_d, 0, SC_COUNT * sizeof(double), h->s);
+  cudaMemsetAsync(h->ctl_d, 0, CT_COUNT * sizeof(int), h->s);
+  cudaMemsetAsync(h->fscal_d, 0, SC_COUNT * sizeof(float), h->s);
+  if ((e = cudaStreamSynchronize(h->s)) != cudaSuccess) { (void)cudaGetLastError(); return cleanup(LES_ERR_CUDA); }
+  *out = h;
+  return LES_OK;
+}
+
+extern "C" int les_gpu_destroy(les_handle *h) {
+  if (!h) return LES_OK;
+  if (h->s) cudaStreamSynchronize(h->s);
+  les_step_plan_free(&h->plan);
+  for (int f = 0; f < kNumFields; ++f) cudaFree(h->fields[f]);
+  cudaFree(h->mask_d);
+  cudaFree(h->g1_d);
+  cudaFree(h->inflow_d);
+  cudaFree(h->cn1_d);
+  cudaFree(h->scal_d);
+  cudaFree(h->ctl_d);
+  cudaFree(h->part_d);
+  cudaFree(h->fscal_d);
+  cudaFree(h->bad_d);
+  if (h->s) cudaStreamDestroy(h->s);
+  (void)cudaGetLastError();
+  delete h;
+  return LES_OK;
+}
+
+namespace {
+
+int check_ext(les_handle *h, int field, const int lb[3], const int ub[3], Ext *decl) {
+  if (!declared_extents(field, h->dims.im, h->dims.jm, h->dims.km, decl))
+    return fail(h, LES_ERR_ARG, "unknown field id " + std::to_string(field));
+  for (int a = 0; a < 3; ++a) {
+    if (lb[a] < decl->lb[a] || ub[a] > decl->ub[a] || ub[a] < lb[a]) {
+      char b[200];
+      snprintf(b, sizeof b, "extents (%d:%d,%d:%d,%d:%d) exceed the declared (%d:%d,%d:%d,%d:%d) of field %d",
+               lb[0], ub[0], lb[1], ub[1], lb[2], ub[2], decl->lb[0], decl->ub[0], decl->lb[1], decl->ub[1],
+               decl->lb[2], decl->ub[2], field);
+      return fail(h, LES_ERR_ARG, b);
+    }
+  }
+  return LES_OK;
+}
+
+cudaMemcpy3DParms copy_parms(les_handle *h, float *dev, float *host, const int lb[3], const int ub[3], bool h2d) {
+  const size_t nx = (size_t)(ub[0] - lb[0] + 1), ny = (size_t)(ub[1] - lb[1] + 1), nz = (size_t)(ub[2] - lb[2] + 1);
+  cudaMemcpy3DParms p;
+  memset(&p, 0, sizeof p);
+  cudaPitchedPtr hp = make_cudaPitchedPtr(host, nx * sizeof(float), nx * sizeof(float), ny);
+  cudaPitchedPtr dp = make_cudaPitchedPtr(dev, (size_t)h->pi * sizeof(float), (size_t)h->pi * sizeof(float), (size_t)h->nj);
+  cudaPos dpos = make_cudaPos((size_t)(lb[0] + LES_IOFF) * sizeof(float), (size_t)(lb[1] + LES_JOFF), (size_t)(lb[2] + LES_KOFF));
+  if (h2d) { p.srcPtr = hp; p.dstPtr = dp; p.dstPos = dpos; p.kind = cudaMemcpyHostToDevice; }
+  else { p.srcPtr = dp; p.srcPos = dpos; p.dstPtr = hp; p.kind = cudaMemcpyDeviceToHost; }
+  p.extent = make_cudaExtent(nx * sizeof(float), ny, nz);
+  return p;
+}
+
+}  // namespace
+
+extern "C" int les_gpu_upload(les_handle *h, int field, const float *host, const int lb[3], const int ub[3]) {
+  if (!h || !host || !lb || !ub) return LES_ERR_ARG;
+  Ext decl;
+  int rc = check_ext(h, field, lb, ub, &decl);
+  if (rc) return rc;
+  const int im = h->dims.im, jm = h->dims.jm, km = h->dims.km;
+  const size_t nx = ub[0] - lb[0] + 1, ny = ub[1] - lb[1] + 1;
+  if (field >= LES_FIELD_U && field <= LES_FIELD_SM) {
+    cudaMemcpy3DParms p = copy_parms(h, h->fields[field - 1], const_cast<float *>(host), lb, ub, true);
+    CK(h, cudaMemcpy3DAsync(&p, h->s));
+    return LES_OK;
+  }
+  if (field >= LES_FIELD_BMASK1 && field <= LES_FIELD_DMASK1) {
+    const uint8_t bit = (uint8_t)(1u << (field - LES_FIELD_BMASK1));
+    for (int k = lb[2]; k <= ub[2]; ++k)
+      for (int j = lb[1]; j <= ub[1]; ++j)
+        for (int i = lb[0]; i <= ub[0]; ++i) {
+          if (i < 1 || i > im || j < 1 || j > jm || k < 1 || k > km) continue;  // halos unused
+          const float x = host[(i - lb[0]) + nx * ((j - lb[1]) + ny * (size_t)(k - lb[2]))];
+          if (x != 0.f && x != 1.f) return fail(h, LES_ERR_ARG, "mask values must be 0 or 1");
+          uint8_t &m = h->mask_h[(size_t)(k + LES_KOFF) * h->np + (size_t)(j + LES_JOFF) * h->pi + (i + LES_IOFF)];
+          m = (uint8_t)(x != 0.f ? (m | bit) : (m & ~bit));
+        }
+    h->mask_dirty = true;
+    return LES_OK;
+  }
+  if (field == LES_FIELD_CN1) {
+    h->cn1_h.assign((size_t)im * jm * km, 0.f);
+    if (lb[0] != 1 || ub[0] != im || lb[1] != 1 || ub[1] != jm || lb[2] != 1 || ub[2] != km)
+      return fail(h, LES_ERR_ARG, "cn1 must be uploaded whole (1:im,1:jm,1:km)");
+    std::copy(host, host + (size_t)im * jm * km, h->cn1_h.begin());
+    h->cn1_given = true;
+    h->committed = false;
+    return LES_OK;
+  }
+  if (field == LES_FIELD_DELX1) return fail(h, LES_ERR_ARG, "delx1 is an output of les (les.f95:38-42)");
+  // 1-D arrays and inflow planes: keep a host copy at the declared extents
+  std::vector<float> &v = h->h1d[field];
+  const size_t dn0 = decl.ub[0] - decl.lb[0] + 1, dn1 = decl.ub[1] - decl.lb[1] + 1;
+  if (v.size() != dn0 * dn1) v.assign(dn0 * dn1, 0.f);
+  for (int j = lb[1]; j <= ub[1]; ++j)
+    for (int i = lb[0]; i <= ub[0]; ++i)
+      v[(i - decl.lb[0]) + dn0 * (size_t)(j - decl.lb[1])] = host[(i - lb[0]) + nx * (size_t)(j - lb[1])];
+  if (is_inflow(field) && h->committed && h->inflow_d) {
+    // inflow planes may change between steps (a time-varying inflow): refresh now
+    const size_t n = (size_t)jm * km;
+    CK(h, cudaMemcpyAsync(h->inflow_d + (size_t)(field - LES_FIELD_UIN) * n, v.data(), n * sizeof(float),
+                          cudaMemcpyHostToDevice, h->s));
+    return LES_OK;
+  }
+  h->committed = false;
+  return LES_OK;
+}
+
+extern "C" int les_gpu_download(les_handle *h, int field, float *host, const int lb[3], const int ub[3]) {
+  if (!h || !host || !lb || !ub) return LES_ERR_ARG;
+  Ext decl;
+  int rc = check_ext(h, field, lb, ub, &decl);
+  if (rc) return rc;
+  if (field >= LES_FIELD_U && field <= LES_FIELD_SM) {
+    cudaMemcpy3DParms p = copy_parms(h, h->fields[field - 1], host, lb, ub, false);
+    CK(h, cudaMemcpy3DAsync(&p, h->s));
+    CK(h, cudaStreamSynchronize(h->s));
+    return LES_OK;
+  }
+  if (field == LES_FIELD_DELX1) {
+    if (!h->committed) return fail(h, LES_ERR_STATE, "delx1 is derived at commit");
+    auto it = h->h1d.find(LES_FIELD_DELX1);
+    for (int i = lb[0]; i <= ub[0]; ++i) host[i - lb[0]] = it->second[i - 1];
+    return LES_OK;
+  }
+  if (is_1d(field) || is_inflow(field)) {
+    auto it = h->h1d.find(field);
+    if (it == h->h1d.end()) return fail(h, LES_ERR_STATE, "field not uploaded");
+    const size_t nx = ub[0] - lb[0] + 1, dn0 = decl.ub[0] - decl.lb[0] + 1;
+    for (int j = lb[1]; j <= ub[1]; ++j)
+      for (int i = lb[0]; i <= ub[0]; ++i)
+        host[(i - lb[0]) + nx * (size_t)(j - lb[1])] = it->second[(i - decl.lb[0]) + dn0 * (size_t)(j - decl.lb[1])];
+    return LES_OK;
+  }
+  return fail(h, LES_ERR_ARG, "field is upload-only");
+}
+
+extern "C" int les_gpu_commit_setup(les_handle *h) {
+  if (!h) return LES_ERR_ARG;
+  const int im = h->dims.im, jm = h->dims.jm, km = h->dims.km;
+  static const int need[] = {LES_FIELD_DX1, LES_FIELD_DY1, LES_FIELD_DZN, LES_FIELD_DZS, LES_FIELD_DXS,
+                             LES_FIELD_DYS, LES_FIELD_CN2L, LES_FIELD_CN2S, LES_FIELD_CN3L, LES_FIELD_CN3S,
+                             LES_FIELD_CN4L, LES_FIELD_CN4S, LES_FIELD_UIN, LES_FIELD_VIN, LES_FIELD_WIN};
+  for (int id : need)
+    if (!h->h1d.count(id)) return fail(h, LES_ERR_STATE, "commit: field " + std::to_string(id) + " not uploaded");
+  auto A = [&](int id, int lo) { return [&h, id, lo](int i) { return h->h1d[id][i - lo]; }; };
+  auto dx1 = A(LES_FIELD_DX1, -1);
+  auto dy1 = A(LES_FIELD_DY1, 0);
+  auto dzn = A(LES_FIELD_DZN, -1);
+  auto dzs = A(LES_FIELD_DZS, -1);
+  auto dxs = A(LES_FIELD_DXS, 0);
+  auto dys = A(LES_FIELD_DYS, 0);
+  // derived constants, evaluated on the host with the same FP32 expressions as the
+  // reference: the log-law factor (vel2.f95:138) and the les length scale (les.f95:41)
+  const float logz = logf(0.5f * dzn(1) / 0.1f);
+  if (!std::isfinite(logz) || logz == 0.f) return fail(h, LES_ERR_ARG, "commit: log(0.5*dzn(1)/0.1) not usable");
+  std::vector<float> delx1(km);
+  for (int k = 1; k <= km; ++k) delx1[k - 1] = powf(dx1(0) * dy1(0) * dzn(k), 1.f / 3.f);
+  h->h1d[LES_FIELD_DELX1] = delx1;
+  // cn1 = 1/(2/(dxs(i-1)dxs(i)) + 2/(dys(j-1)dys(j)) + 2/(dzs(k-1)dzs(k))) (init.f95:98-104)
+  std::vector<float> ca(im + 1), cb(jm + 1), cc(km + 1), ck(km + 1, 0.f);
+  for (int i = 1; i <= im; ++i) ca[i] = 2.f / (dxs(i - 1) * dxs(i));
+  for (int j = 1; j <= jm; ++j) cb[j] = 2.f / (dys(j - 1) * dys(j));
+  for (int k = 1; k <= km; ++k) cc[k] = 2.f / (dzs(k - 1) * dzs(k));
+  bool uniform = true;
+  for (int i = 2; i <= im; ++i) uniform = uniform && (ca[i] == ca[1]);
+  for (int j = 2; j <= jm; ++j) uniform = uniform && (cb[j] == cb[1]);
+  if (uniform)
+    for (int k = 1; k <= km; ++k) ck[k] = 1.f / (ca[1] + cb[1] + cc[k]);
+  bool need_cn1 = false;
+  if (h->cn1_given) {
+    for (int k = 1; k <= km && !need_cn1; ++k)
+      for (int j = 1; j <= jm && !need_cn1; ++j)
+        for (int i = 1; i <= im; ++i) {
+          const float f = 1.f / (ca[i] + cb[j] + cc[k]);
+          const float g = h->cn1_h[(size_t)(i - 1) + (size_t)(j - 1) * im + (size_t)(k - 1) * im * jm];
+          if (memcmp(&f, &g, 4) != 0) { need_cn1 = true; break; }
+        }
+  }
+  // 1-D device buffer: [dx1 dy1 dzn dzs dxs dys z2 cn2l cn2s cn3l cn3s cn4l cn4s delx1 ca cb cc ck]
+  struct Seg { int id; int lo; int n; const float *src; };
+  std::vector<float> z2v(km + 3, 0.f);
+  if (h->h1d.count(LES_FIELD_Z2)) z2v = h->h1d[LES_FIELD_Z2];
+  std::vector<Seg> segs = {
+      {LES_FIELD_DX1, -1, im + 3, h->h1d[LES_FIELD_DX1].data()}, {LES_FIELD_DY1, 0, jm + 2, h->h1d[LES_FIELD_DY1].data()},
+      {LES_FIELD_DZN, -1, km + 4, h->h1d[LES_FIELD_DZN].data()}, {LES_FIELD_DZS, -1, km + 4, h->h1d[LES_FIELD_DZS].data()},
+      {LES_FIELD_DXS, 0, im + 1, h->h1d[LES_FIELD_DXS].data()},  {LES_FIELD_DYS, 0, jm + 1, h->h1d[LES_FIELD_DYS].data()},
+      {LES_FIELD_Z2, 0, km + 3, z2v.data()},
+      {LES_FIELD_CN2L, 1, im, h->h1d[LES_FIELD_CN2L].data()},    {LES_FIELD_CN2S, 1, im, h->h1d[LES_FIELD_CN2S].data()},
+      {LES_FIELD_CN3L, 1, jm, h->h1d[LES_FIELD_CN3L].data()},    {LES_FIELD_CN3S, 1, jm, h->h1d[LES_FIELD_CN3S].data()},
+      {LES_FIELD_CN4L, 1, km, h->h1d[LES_FIELD_CN4L].data()},    {LES_FIELD_CN4S, 1, km, h->h1d[LES_FIELD_CN4S].data()},
+      {LES_FIELD_DELX1, 1, km, h->h1d[LES_FIELD_DELX1].data()},
+      {-1, 0, im + 1, ca.data()}, {-2, 0, jm + 1, cb.data()}, {-3, 0, km + 1, cc.data()}, {-4, 0, km + 1, ck.data()}};
+  size_t total = 0;
+  std::vector<size_t> off(segs.size());
+  for (size_t q = 0; q < segs.size(); ++q) { off[q] = total; total += (segs[q].n + 7) / 8 * 8; }
+  std::vector<float> buf(total, 0.f);
+  for (size_t q = 0; q < segs.size(); ++q) std::copy(segs[q].src, segs[q].src + segs[q].n, buf.begin() + off[q]);
+  CK(h, cudaStreamSynchronize(h->s));
+  cudaFree(h->g1_d); h->g1_d = nullptr;
+  CK(h, cudaMalloc(&h->g1_d, total * sizeof(float)));
+  CK(h, cudaMemcpyAsync(h->g1_d, buf.data(), total * sizeof(float), cudaMemcpyHostToDevice, h->s));
+  auto P = [&](size_t q) { return (const float *)(h->g1_d + off[q] - segs[q].lo); };
+  LesGrid1 g;
+  g.dx1 = P(0); g.dy1 = P(1); g.dzn = P(2); g.dzs = P(3); g.dxs = P(4); g.dys = P(5); g.z2 = P(6);
+  g.cn2l = P(7); g.cn2s = P(8); g.cn3l = P(9); g.cn3s = P(10); g.cn4l = P(11); g.cn4s = P(12); g.delx1 = P(13);
+  g.cn1a = P(14); g.cn1b = P(15); g.cn1c = P(16); g.cn1k = uniform ? P(17) : nullptr;
+  // full cn1 only if the uploaded one is not the separable formula bit for bit
+  cudaFree(h->cn1_d); h->cn1_d = nullptr;
+  if (need_cn1) {
+    CK(h, cudaMalloc(&h->cn1_d, h->cn1_h.size() * sizeof(float)));
+    CK(h, cudaMemcpyAsync(h->cn1_d, h->cn1_h.data(), h->cn1_h.size() * sizeof(float), cudaMemcpyHostToDevice, h->s));
+  }
+  // inflow planes
+  const size_t nin = (size_t)jm * km;
+  cudaFree(h->inflow_d); h->inflow_d = nullptr;
+  CK(h, cudaMalloc(&h->inflow_d, 3 * nin * sizeof(float)));
+  for (int q = 0; q < 3; ++q)
+    CK(h, cudaMemcpyAsync(h->inflow_d + q * nin, h->h1d[LES_FIELD_UIN + q].data(), nin * sizeof(float),
+                          cudaMemcpyHostToDevice, h->s));
+  // masks
+  if (h->mask_dirty) {
+    CK(h, cudaMemcpyAsync(h->mask_d, h->mask_h.data(), h->nfloat, cudaMemcpyHostToDevice, h->s));
+    h->mask_dirty = false;
+  }
+  // sum of cell volumes in FP64, sequential in the reference's loop order (press.f95:65-72)
+  double area = 0.0;
+  for (int k = 1; k <= km; ++k)
+    for (int j = 1; j <= jm; ++j)
+      for (int i = 1; i <= im; ++i) area += (double)(dx1(i) * dy1(j) * dzn(k));
+  CK(h, cudaMemcpyAsync(h->scal_d + SC_AREA, &area, sizeof(double), cudaMemcpyHostToDevice, h->s));
+  CK(h, cudaStreamSynchronize(h->s));
+  // domain view
+  LesDom &d = h->dom;
+  d.im = im; d.jm = jm; d.km = km; d.pi = h->pi; d.nj = h->nj; d.np = h->np;
+  float **F = h->fields;
+  d.u = F[0]; d.v = F[1]; d.w = F[2]; d.p = F[3]; d.f = F[4]; d.g = F[5]; d.h = F[6];
+  d.fold = F[7]; d.gold = F[8]; d.hold = F[9]; d.usum = F[10]; d.vsum = F[11]; d.wsum = F[12];
+  d.rhs = F[13]; d.sm = F[14];
+  d.cn1 = h->cn1_d;
+  d.mask = h->mask_d;
+  d.uin = h->inflow_d; d.vin = h->inflow_d + nin; d.win = h->inflow_d + 2 * nin;
+  d.gr = g;
+  d.dt = h->prm.dt; d.ro = h->prm.ro; d.vn = h->prm.vn; d.alpha = h->prm.alpha; d.beta = h->prm.beta;
+  d.omega = h->prm.omega; d.pjuge = h->prm.pjuge;
+  d.logz = logz;
+  d.sor_fixed = h->prm.sor_fixed;
+  d.scal = h->scal_d; d.ctl = h->ctl_d; d.part = h->part_d; d.fscal = h->fscal_d;
+  les_step_plan_free(&h->plan);
+  h->committed = true;
+  return LES_OK;
+}
+
+extern "C" int les_gpu_setup_scenario(les_handle *h, const les_scenario *sc) {
+  if (!h || !sc) return LES_ERR_ARG;
+  const int im = h->dims.im, jm = h->dims.jm, km = h->dims.km;
+  if (sc->im != im || sc->jm != jm || sc->km != km) return fail(h, LES_ERR_ARG, "scenario dims differ from handle dims");
+  std::vector<float> dx1(im + 3), dxl(im + 1), dxs(im + 1), dy1(jm + 2), dyl(jm + 1), dys(jm + 1), dzn(km + 4),
+      dzs(km + 4), z2(km + 3);
+  int rc = les_setup_grid(im, jm, km, sc->dx, sc->dy, sc->dz_law, sc->dz0, sc->dz_ratio, dx1.data(), dxl.data(),
+                          dxs.data(), dy1.data(), dyl.data(), dys.data(), dzn.data(), dzs.data(), z2.data());
+  if (rc) return fail(h, rc, "les_setup_grid failed");
+  std::vector<float> cn2s(im), cn2l(im), cn3s(jm), cn3l(jm), cn4s(km), cn4l(km);
+  rc = les_setup_poisson(im, jm, km, dxs.data(), dys.data(), dzs.data(), cn2s.data(), cn2l.data(), cn3s.data(),
+                         cn3l.data(), cn4s.data(), cn4l.data(), nullptr);
+  if (rc) return fail(h, rc, "les_setup_poisson failed");
+  std::vector<float> zbm((size_t)im * jm), uin((size_t)jm * km), vin((size_t)jm * km), win((size_t)jm * km);
+  rc = les_scenario_generate(sc, zbm.data(), uin.data(), vin.data(), win.data());
+  if (rc) return fail(h, rc, "les_scenario_generate failed");
+  std::vector<float> dm((size_t)(im + 2) * (jm + 2) * (km + 2));
+  rc = les_setup_masks(im, jm, km, zbm.data(), z2.data(), dzn.data(), nullptr, nullptr, nullptr, dm.data());
+  if (rc) return fail(h, rc, "les_setup_masks failed");
+  struct U1 { int id; const float *p; int lo, hi; };
+  const U1 ones[] = {{LES_FIELD_DX1, dx1.data(), -1, im + 1}, {LES_FIELD_DY1, dy1.data(), 0, jm + 1},
+                     {LES_FIELD_DZN, dzn.data(), -1, km + 2}, {LES_FIELD_DZS, dzs.data(), -1, km + 2},
+                     {LES_FIELD_DXS, dxs.data(), 0, im},      {LES_FIELD_DYS, dys.data(), 0, jm},
+                     {LES_FIELD_Z2, z2.data(), 0, km + 2},    {LES_FIELD_CN2L, cn2l.data(), 1, im},
+                     {LES_FIELD_CN2S, cn2s.data(), 1, im},    {LES_FIELD_CN3L, cn3l.data(), 1, jm},
+                     {LES_FIELD_CN3S, cn3s.data(), 1, jm},    {LES_FIELD_CN4L, cn4l.data(), 1, km},
+                     {LES_FIELD_CN4S, cn4s.data(), 1, km}};
+  for (const U1 &u : ones) {
+    const int lb[3] = {u.lo, 0, 0}, ub[3] = {u.hi, 0, 0};
+    if ((rc = les_gpu_upload(h, u.id, u.p, lb, ub))) return rc;
+  }
+  const int lbi[3] = {1, 1, 0}, ubi[3] = {jm, km, 0};
+  if ((rc = les_gpu_upload(h, LES_FIELD_UIN, uin.data(), lbi, ubi))) return rc;
+  if ((rc = les_gpu_upload(h, LES_FIELD_VIN, vin.data(), lbi, ubi))) return rc;
+  if ((rc = les_gpu_upload(h, LES_FIELD_WIN, win.data(), lbi, ubi))) return rc;
+  // b, c, d masks are equal on the interior (feedbfm.f95:106-116)
+  const int lbm[3] = {0, 0, 0}, ubm[3] = {im + 1, jm + 1, km + 1};
+  for (int f = LES_FIELD_BMASK1; f <= LES_FIELD_DMASK1; ++f)
+    if ((rc = les_gpu_upload(h, f, dm.data(), lbm, ubm))) return rc;
+  return les_gpu_commit_setup(h);
+}
+
+#define NEED_COMMIT(h)                                                                     \
+  do {                                                                                     \
+    if (!(h)) return LES_ERR_ARG;                                                          \
+    if (!(h)->committed) return fail((h), LES_ERR_STATE, "les_gpu_commit_setup not called"); \
+  } while (0)
+
+extern "C" int les_gpu_velnw(les_handle *h) {
+  NEED_COMMIT(h);
+  les_launch_velnw(h->dom, ctx_of(h));
+  return check_launch(h, "velnw");
+}
+extern "C" int les_gpu_bondv1(les_handle *h, int n) {
+  NEED_COMMIT(h);
+  les_launch_bondv1(h->dom, n, ctx_of(h));
+  return check_launch(h, "bondv1");
+}
+extern "C" int les_gpu_velfg(les_handle *h) {
+  NEED_COMMIT(h);
+  les_launch_velfg(h->dom, ctx_of(h));
+  return check_launch(h, "velfg");
+}
+extern "C" int les_gpu_feedbf(les_handle *h) {
+  NEED_COMMIT(h);
+  les_launch_feedbf(h->dom, ctx_of(h));
+  return check_launch(h, "feedbf");
+}
+extern "C" int les_gpu_les(les_handle *h) {
+  NEED_COMMIT(h);
+  les_launch_les(h->dom, ctx_of(h));
+  return check_launch(h, "les");
+}
+extern "C" int les_gpu_adam(les_handle *h) {
+  NEED_COMMIT(h);
+  les_launch_adam(h->dom, ctx_of(h));
+  return check_launch(h, "adam");
+}
+extern "C" int les_gpu_bondfg(les_handle *h) {
+  NEED_COMMIT(h);
+  les_launch_bondfg(h->dom, ctx_of(h));
+  return check_launch(h, "bondfg");
+}
+extern "C" int les_gpu_boundp1(les_handle *h) {
+  NEED_COMMIT(h);
+  les_launch_boundp1(h->dom, ctx_of(h), 0);
+  return check_launch(h, "boundp1");
+}
+extern "C" int les_gpu_boundp2(les_handle *h) {
+  NEED_COMMIT(h);
+  les_launch_boundp2(h->dom, ctx_of(h), 0);
+  return check_launch(h, "boundp2");
+}
+extern "C" int les_gpu_press(les_handle *h, int n, int nmax) {
+  NEED_COMMIT(h);
+  (void)n; (void)nmax;
+  LesCtx c = ctx_of(h);
+  les_launch_bondfg(h->dom, c);
+  les_launch_rhs_mean(h->dom, c);
+  les_launch_sor_simple(h->dom, h->prm.nmaxp, c);
+  les_launch_pav_adjust(h->dom, c);
+  return check_launch(h, "press");
+}
+
+extern "C" int les_gpu_step(les_handle *h, int n, int nmax) {
+  NEED_COMMIT(h);
+  int rc = les_step_run(h->dom, h->prm, &h->plan, n, nmax, ctx_of(h));
+  if (rc) return fail(h, LES_ERR_CUDA, std::string("step: ") + cudaGetErrorString(cudaGetLastError()));
+  return check_launch(h, "step");
+}
+
+extern "C" int les_gpu_run(les_handle *h, int n0, int nsteps, int nmax) {
+  NEED_COMMIT(h);
+  for (int n = n0; n < n0 + nsteps; ++n) {
+    int rc = les_gpu_step(h, n, nmax);
+    if (rc) return rc;
+  }
+  return LES_OK;
+}
+
+extern "C" int les_gpu_sync(les_handle *h) {
+  if (!h) return LES_ERR_ARG;
+  CK(h, cudaStreamSynchronize(h->s));
+  return LES_OK;
+}
+
+extern "C" int les_gpu_diag(les_handle *h, double out[5]) {
+  if (!h || !out) return LES_ERR_ARG;
+  double sc[SC_COUNT];
+  int ct[CT_COUNT];
+  CK(h, cudaMemcpyAsync(sc, h->scal_d, sizeof sc, cudaMemcpyDeviceToHost, h->s));
+  CK(h, cudaMemcpyAsync(ct, h->ctl_d, sizeof ct, cudaMemcpyDeviceToHost, h->s));
+  CK(h, cudaStreamSynchronize(h->s));
+  out[0] = ct[CT_ITERS];
+  out[1] = sc[SC_SOR];
+  out[2] = sc[SC_UOUT];
+  out[3] = sc[SC_RHSAV];
+  out[4] = sc[SC_PAV];
+  return LES_OK;
+}
+
+extern "C" int les_gpu_check_finite(les_handle *h, long long *bad) {
+  NEED_COMMIT(h);
+  if (!bad) return LES_ERR_ARG;
+  CK(h, cudaMemsetAsync(h->bad_d, 0, sizeof(unsigned long long), h->s));
+  les_launch_count_nonfinite(h->dom, h->bad_d, ctx_of(h));
+  int rc = check_launch(h, "check_finite");
+  if (rc) return rc;
+  unsigned long long b = 0;
+  CK(h, cudaMemcpyAsync(&b, h->bad_d, sizeof b, cudaMemcpyDeviceToHost, h->s));
+  CK(h, cudaStreamSynchronize(h->s));
+  *bad = (long long)b;
+  return b ? LES_ERR_NUMERIC : LES_OK;
+}
+
+extern "C" int les_gpu_stream(les_handle *h, void **stream) {
+  if (!h || !stream) return LES_ERR_ARG;
+  *stream = (void *)h->s;
+  return LES_OK;
+}
+
+extern "C" long long les_gpu_launch_count(les_handle *h) { return h ? h->nlaunch : -1; }
+
+extern "C" int les_gpu_last_error(les_handle *h, char *buf, size_t len) {
+  if (!h || !buf || len == 0) return LES_ERR_ARG;
+  snprintf(buf, len, "%s", h->err.c_str());
+  return LES_OK;
+}
+
+extern "C" int les_gpu_profile(les_handle *h, int what, int reps, double *ms_avg) {
+  NEED_COMMIT(h);
+  if (!ms_avg || reps < 1) return LES_ERR_ARG;
+  cudaEvent_t a, b;
+  CK(h, cudaEventCreate(&a));
+  CK(h, cudaEventCreate(&b));
+  LesCtx c = ctx_of(h);
+  CK(h, cudaEventRecord(a, h->s));
+  for (int r = 0; r < reps; ++r) {
+    switch (what) {
+      case LES_PROF_SOR: les_step_sor_pass(h->dom, h->prm, &h->plan, c); break;
+      case LES_PROF_VELFG: les_step_velfg_pass(h->dom, c); break;
+      case LES_PROF_LES: les_step_les_pass(h->dom, c); break;
+      case LES_PROF_VELNW: les_launch_velnw(h->dom, c); break;
+      case LES_PROF_STEP: {
+        int rc = les_step_run(h->dom, h->prm, &h->plan, 2, 2, c);
+        if (rc) return fail(h, LES_ERR_CUDA, "profile: step failed");
+        break;
+      }
+      default: cudaEventDestroy(a); cudaEventDestroy(b); return fail(h, LES_ERR_ARG, "profile: unknown stage");
+    }
+  }
+  CK(h, cudaEventRecord(b, h->s));
+  CK(h, cudaEventSynchronize(b));
+  float ms = 0.f;
+  CK(h, cudaEventElapsedTime(&ms, a, b));
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  *ms_avg = (double)ms / reps;
+  return check_launch(h, "profile");
+}

@@ -1,0 +1,28 @@
+// les_kernels.cuh -- host-side launchers of the solver kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "les_common.cuh"
+
+// Launch context: the stream work goes to and the counter of kernel launches.
+struct LesCtx {
+  cudaStream_t s;
+  long long *nlaunch;
+};
+
+// per-subroutine kernels (les_kernels.cu)
+void les_launch_velnw(const LesDom &d, LesCtx ctx);
+void les_launch_bondv1(const LesDom &d, int n, LesCtx ctx);
+void les_launch_velfg(const LesDom &d, LesCtx ctx);
+void les_launch_feedbf(const LesDom &d, LesCtx ctx);
+void les_launch_les(const LesDom &d, LesCtx ctx);
+void les_launch_adam(const LesDom &d, LesCtx ctx);
+void les_launch_bondfg(const LesDom &d, LesCtx ctx);
+void les_launch_boundp1(const LesDom &d, LesCtx ctx, int obey_converged);
+void les_launch_boundp2(const LesDom &d, LesCtx ctx, int obey_converged);
+void les_launch_rhs_mean(const LesDom &d, LesCtx ctx);
+void les_launch_sor_simple(const LesDom &d, int nmaxp, LesCtx ctx);
+void les_launch_pav_adjust(const LesDom &d, LesCtx ctx);
+void les_launch_count_nonfinite(const LesDom &d, unsigned long long *bad, LesCtx ctx);
+int les_interior_blocks(const LesDom &d);
+int les_sor_simple_parts(const LesDom &d);

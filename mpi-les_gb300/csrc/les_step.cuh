@@ -1,0 +1,25 @@
+// les_step.cuh -- the whole time step (main.f95:260-296) as one launch sequence.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "../../include/les_gpu.h"
+#include "les_common.cuh"
+#include "les_kernels.cuh"
+
+// Captured CUDA graphs of one step: [0] for n == 1 (bondv1's initial fill), [1] for n > 1.
+struct LesStepPlan {
+  cudaGraphExec_t exec[2] = {nullptr, nullptr};
+  long long launches[2] = {0, 0};  // kernels inside each graph
+  int sor_depth = 0;               // SOR iterations fused per pass chosen for this domain
+};
+
+int les_step_parts_needed(int im, int jm, int km);
+void les_step_plan_free(LesStepPlan *plan);
+// Queue one step on ctx.s.  Returns 0 or a CUDA error code.
+int les_step_run(const LesDom &d, const les_params &prm, LesStepPlan *plan, int n, int nmax, LesCtx ctx);
+// Single passes of the step's heavy kernels, for profiling (les_gpu_profile).
+void les_step_sor_pass(const LesDom &d, const les_params &prm, LesStepPlan *plan, LesCtx ctx);
+void les_step_velfg_pass(const LesDom &d, LesCtx ctx);
+void les_step_les_pass(const LesDom &d, LesCtx ctx);
+// The launch sequence itself (no graph), used for capture and by tests.
+void les_step_enqueue(const LesDom &d, const les_params &prm, int sor_depth, int n, LesCtx ctx);

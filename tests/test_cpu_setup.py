@@ -1,0 +1,117 @@
+"""CPU checks: the product's host set-up against the oracle, and the C-ABI surface.
+
+No GPU needed: the set-up routines (grid.f95, init.f95:82-107, feedbfm.f95) and the
+scenario generator are host code of the solver library.
+"""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+import lesgpu
+from helpers import make_ref, scenario
+from oracle import ref
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared_functions(header):
+    src = open(header).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    names = re.findall(r"^\s*(?:[A-Za-z_][\w\s\*]*?)\b(les_\w+)\s*\(", src, flags=re.M)
+    return sorted(set(names))
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    lib = C.CDLL(built_lib)
+    names = _declared_functions(os.path.join(ROOT, "include", "les_gpu.h"))
+    assert len(names) >= 25
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_field_ids_match_oracle(built_lib):
+    sc = scenario(12, 8, 6)
+    r = make_ref(4, sc)
+    for fid in list(lesgpu.FIELD_NAMES) + [lesgpu.BMASK1, lesgpu.CMASK1, lesgpu.DMASK1, lesgpu.CN1]:
+        lb, ub = lesgpu.declared_extents(fid, sc.im, sc.jm, sc.km)
+        assert r.extents(fid) == (lb, ub), fid
+    for fid in (lesgpu.DX1, lesgpu.DY1, lesgpu.DZN, lesgpu.DZS, lesgpu.DXS, lesgpu.DYS, lesgpu.Z2, lesgpu.CN2L,
+                lesgpu.CN2S, lesgpu.CN3L, lesgpu.CN3S, lesgpu.CN4L, lesgpu.CN4S, lesgpu.DELX1):
+        lb, ub = lesgpu.declared_extents(fid, sc.im, sc.jm, sc.km)
+        rl, ru = r.extents(fid)
+        assert (rl[0], ru[0]) == (lb[0], ub[0]), fid
+
+
+@pytest.mark.parametrize("dz_law,km", [(1, 20), (1, 90), (0, 64)])
+def test_grid_matches_oracle(built_lib, dz_law, km):
+    im, jm = 30, 20
+    g = lesgpu.setup_grid(im, jm, km, dz_law=dz_law)
+    sc = scenario(im, jm, km, dz_law=dz_law)
+    r = make_ref(4, sc)
+    for name, fid in (("dx1", lesgpu.DX1), ("dy1", lesgpu.DY1), ("dzn", lesgpu.DZN), ("dzs", lesgpu.DZS),
+                      ("dxs", lesgpu.DXS), ("dys", lesgpu.DYS), ("z2", lesgpu.Z2)):
+        o = r.get(fid).ravel(order="F").astype(np.float32)
+        assert np.array_equal(g[name].view(np.uint32), o.view(np.uint32)), name
+
+
+def test_poisson_and_masks_match_oracle(built_lib):
+    im, jm, km = 26, 18, 22
+    sc = scenario(im, jm, km, seed=4, coverage=0.4)
+    g = lesgpu.setup_grid(im, jm, km)
+    lib = lesgpu.load_library()
+    fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+    cn = {n: np.zeros(s, np.float32) for n, s in (("cn2s", im), ("cn2l", im), ("cn3s", jm), ("cn3l", jm),
+                                                  ("cn4s", km), ("cn4l", km))}
+    cn1 = np.zeros((im, jm, km), np.float32, order="F")
+    assert lib.les_setup_poisson(im, jm, km, fp(g["dxs"]), fp(g["dys"]), fp(g["dzs"]), fp(cn["cn2s"]),
+                                 fp(cn["cn2l"]), fp(cn["cn3s"]), fp(cn["cn3l"]), fp(cn["cn4s"]), fp(cn["cn4l"]),
+                                 fp(cn1)) == 0
+    r = make_ref(4, sc)
+    for name, fid in (("cn2s", lesgpu.CN2S), ("cn2l", lesgpu.CN2L), ("cn3s", lesgpu.CN3S), ("cn3l", lesgpu.CN3L),
+                      ("cn4s", lesgpu.CN4S), ("cn4l", lesgpu.CN4L)):
+        o = r.get(fid).ravel(order="F").astype(np.float32)
+        assert np.array_equal(cn[name].view(np.uint32), o.view(np.uint32)), name
+    assert np.array_equal(cn1.view(np.uint32), r.get(lesgpu.CN1).astype(np.float32).view(np.uint32))
+    zbm, uin, vin, win = lesgpu.generate_scenario(sc)
+    masks = {n: np.zeros(s, np.float32, order="F") for n, s in (
+        ("a", (im + 2, jm + 2, km + 2)), ("b", (im + 3, jm + 2, km + 2)), ("c", (im + 2, jm + 3, km + 2)),
+        ("d", (im + 2, jm + 2, km + 2)))}
+    assert lib.les_setup_masks(im, jm, km, fp(zbm), fp(g["z2"]), fp(g["dzn"]), fp(masks["a"]), fp(masks["b"]),
+                               fp(masks["c"]), fp(masks["d"])) == 0
+    for n, fid in (("a", 19), ("b", lesgpu.BMASK1), ("c", lesgpu.CMASK1), ("d", lesgpu.DMASK1)):
+        assert np.array_equal(masks[n], r.get(fid).astype(np.float32)), n
+    assert 0.0 < masks["d"][1:-1, 1:-1, 1:-1].mean() < 1.0
+
+
+def test_scenario_generator_is_deterministic_and_in_range(built_lib):
+    sc = scenario(96, 64, 48, seed=17, coverage=0.3)
+    a = lesgpu.generate_scenario(sc)
+    b = lesgpu.generate_scenario(sc)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+    zbm, uin, vin, win = a
+    cov = (zbm > 0).mean()
+    assert 0.3 <= cov <= 0.45, cov
+    assert zbm.max() <= 60.0 and zbm[zbm > 0].min() >= 10.0
+    assert np.all(zbm[: 96 // 8 - 1, :] == 0) and np.all(zbm[96 - 96 // 8:, :] == 0)
+    # power law u = 5 (z/100)^0.2 with z = z2(k) + 0.5 dzn(k), noise within +-1e-3
+    g = lesgpu.setup_grid(96, 64, 48)
+    z = g["z2"][1:49].astype(np.float64) + 0.5 * g["dzn"][2:50].astype(np.float64)
+    u = 5.0 * (z / 100.0) ** 0.2
+    assert np.abs(uin - u[None, :]).max() <= 1.01e-3
+    assert np.abs(vin).max() <= 1.01e-3 and np.abs(win).max() <= 1.01e-3
+    c = lesgpu.generate_scenario(scenario(96, 64, 48, seed=18))
+    assert not np.array_equal(c[0], zbm)
+
+
+def test_direction_rotates_inflow(built_lib):
+    sc = scenario(40, 32, 20, seed=3, direction_deg=30.0, noise=0.0)
+    _, uin, vin, _ = lesgpu.generate_scenario(sc)
+    ang = np.degrees(np.arctan2(vin, uin))
+    assert np.allclose(ang, 30.0, atol=1e-3)
+    sc2 = scenario(40, 32, 20, seed=3, direction_deg=120.0, noise=0.0)
+    _, u2, v2, _ = lesgpu.generate_scenario(sc2)
+    assert np.allclose(np.degrees(np.arctan2(v2, u2)), 30.0, atol=1e-3)

@@ -1,0 +1,90 @@
+"""Whole-step parity: the GPU time loop against the FP32 and FP64 oracles.
+
+The parity contract: after N steps, err(x) = max|x - x_ref| / max|x_ref| over the
+interior is <= 1e-4 for u, v, w and p against the FP64 oracle.  Against the FP32
+oracle the GPU is exact except for the order of the FP64 sums (rhsav, pav) and,
+with the oracle in gfortran mode, glibc's powf(x, 0.5) for x**0.5; the tighter
+tolerances below bound those.
+"""
+import numpy as np
+import pytest
+
+import lesgpu
+from helpers import make_gpu, make_ref, rel_err, scenario
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ((lesgpu.U, "u"), (lesgpu.V, "v"), (lesgpu.W, "w"), (lesgpu.P, "p"))
+
+
+def _interior(obj, fid, sc, gpu):
+    lb, ub = (1, 1, 1), (sc.im, sc.jm, sc.km)
+    if gpu:
+        return obj.download(fid, lb, ub).astype(np.float64)
+    return obj.get(fid, lb, ub)
+
+
+def _run_pair(sc, nsteps, params, prec, **rkw):
+    gpu = make_gpu(sc, params)
+    orc = make_ref(prec, sc, params, **rkw)
+    for n in range(1, nsteps + 1):
+        gpu.step(n, nsteps)
+        orc.step(n, nsteps)
+    gpu.sync()
+    return gpu, orc
+
+
+def test_step_matches_stage_sequence(built_lib):
+    """The fused/graph step equals the per-subroutine entry points bit for bit."""
+    sc = scenario(48, 32, 16, seed=9)
+    params = lesgpu.Params(nmaxp=20)
+    a = make_gpu(sc, params)
+    b = make_gpu(sc, params)
+    for n in range(1, 5):
+        a.step(n, 4)
+        b.velnw(); b.bondv1(n); b.velfg(); b.feedbf(); b.les(); b.adam(); b.press(n, 4)
+    for fid in lesgpu.STATE_FIELDS:
+        x, y = a.download(fid), b.download(fid)
+        assert np.array_equal(x.view(np.uint32), y.view(np.uint32)), lesgpu.FIELD_NAMES[fid]
+
+
+@pytest.mark.parametrize("shape,nsteps", [((48, 32, 24), 10), ((40, 64, 20), 6)])
+def test_steps_vs_fp32_oracle(built_lib, shape, nsteps):
+    sc = scenario(*shape, seed=21)
+    params = lesgpu.Params()
+    gpu, orc = _run_pair(sc, nsteps, params, 4, sqrt_half=1, red64=1)
+    for fid, nm in FIELDS:
+        e = rel_err(_interior(gpu, fid, sc, True), _interior(orc, fid, sc, False))
+        assert e <= 1e-5, (nm, e)
+    assert gpu.diag()["iters"] == orc.diag()["iters"]
+
+
+@pytest.mark.parametrize("shape,nsteps", [((48, 32, 24), 10)])
+def test_steps_vs_fp64_oracle(built_lib, shape, nsteps):
+    sc = scenario(*shape, seed=22)
+    params = lesgpu.Params()
+    gpu, orc = _run_pair(sc, nsteps, params, 8, sqrt_half=0, red64=1)
+    for fid, nm in FIELDS:
+        e = rel_err(_interior(gpu, fid, sc, True), _interior(orc, fid, sc, False))
+        assert e <= 1e-4, (nm, e)
+
+
+def test_steps_vs_gfortran_semantics(built_lib):
+    """Oracle with powf(x,0.5) and sequential FP32 sums, exactly as the reference."""
+    sc = scenario(48, 32, 24, seed=23)
+    params = lesgpu.Params()
+    gpu, orc = _run_pair(sc, 8, params, 4, sqrt_half=0, red64=0)
+    for fid, nm in FIELDS:
+        e = rel_err(_interior(gpu, fid, sc, True), _interior(orc, fid, sc, False))
+        assert e <= 1e-4, (nm, e)
+
+
+@pytest.mark.slow
+def test_plain_small_config_vs_fp64(built_lib):
+    """The plain small configuration: 150x150x90, 20 steps, 50 SOR iterations."""
+    sc = scenario(150, 150, 90, seed=1)
+    params = lesgpu.Params()
+    gpu, orc = _run_pair(sc, 20, params, 8, sqrt_half=0, red64=1, fast=True)
+    errs = {nm: rel_err(_interior(gpu, fid, sc, True), _interior(orc, fid, sc, False)) for fid, nm in FIELDS}
+    assert max(errs.values()) <= 1e-4, errs
+    assert gpu.nonfinite() == 0
