@@ -85,6 +85,12 @@ struct les_handle {
   double *part_d = nullptr;
   float *fscal_d = nullptr;
   unsigned long long *bad_d = nullptr;
+  float *sor_d[3] = {};           // internal buffers of the fused SOR sweep (A, B, rhs)
+  unsigned int *cnt_d = nullptr;  // CTA ticket of the fused SOR sweep
+  int sms = 0;
+  // p's i/j halos may disagree with its interior (set by an upload of p, cleared by
+  // press): the next step then runs the per-subroutine kernels, exact for any state
+  bool p_dirty = false;
   size_t npart = 0;
   bool committed = false;
   LesDom dom{};
@@ -128,7 +134,7 @@ extern "C" size_t les_domain_bytes(int im, int jm, int km) {
   const size_t pi = (size_t)pitch_for(im), nj = (size_t)jm + 4, nk = (size_t)km + 4;
   const size_t field = pi * nj * nk * sizeof(float);
   const size_t part = ((size_t)(im + 63) / 64 + 1) * ((size_t)(jm + 3) / 4 + 1) * (size_t)km * 2 * sizeof(double);
-  return kNumFields * field + pi * nj * nk /*mask bytes*/ + part + 64 * 1024;
+  return (kNumFields + 3) * field + pi * nj * nk /*mask bytes*/ + part + 64 * 1024;
 }
 
 extern "C" int les_gpu_create(const les_dims *dims, const les_params *params, les_handle **out) {
@@ -166,6 +172,23 @@ extern "C" int les_gpu_create(const les_dims *dims, const les_params *params, le
     }
   }
   if (cudaMalloc(&h->mask_d, h->nfloat) != cudaSuccess) { (void)cudaGetLastError(); return cleanup(LES_ERR_NOMEM); }
+  for (int q = 0; q < 3; ++q) {
+    if (cudaMalloc(&h->sor_d[q], h->nfloat * sizeof(float)) != cudaSuccess) {
+      (void)cudaGetLastError();
+      return cleanup(LES_ERR_NOMEM);
+    }
+    cudaMemsetAsync(h->sor_d[q], 0, h->nfloat * sizeof(float), h->s);
+  }
+  if (cudaMalloc(&h->cnt_d, 64) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return cleanup(LES_ERR_NOMEM);
+  }
+  cudaMemsetAsync(h->cnt_d, 0, 64, h->s);
+  cudaMemsetAsync(h->mask_d, 0, h->nfloat, h->s);
+  if (cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, h->dev) != cudaSuccess) {
+    (void)cudaGetLastError();
+    h->sms = 0;
+  }
   h->mask_h.assign(h->nfloat, 0);
   // partial-sum buffer: the largest per-block count of any reduction kernel
   h->npart = (size_t)std::max<long long>(
@@ -200,6 +223,8 @@ extern "C" int les_gpu_destroy(les_handle *h) {
   cudaFree(h->part_d);
   cudaFree(h->fscal_d);
   cudaFree(h->bad_d);
+  for (int q = 0; q < 3; ++q) cudaFree(h->sor_d[q]);
+  cudaFree(h->cnt_d);
   if (h->s) cudaStreamDestroy(h->s);
   (void)cudaGetLastError();
   delete h;
@@ -248,6 +273,7 @@ extern "C" int les_gpu_upload(les_handle *h, int field, const float *host, const
   if (field >= LES_FIELD_U && field <= LES_FIELD_SM) {
     cudaMemcpy3DParms p = copy_parms(h, h->fields[field - 1], const_cast<float *>(host), lb, ub, true);
     CK(h, cudaMemcpy3DAsync(&p, h->s));
+    if (field == LES_FIELD_P) h->p_dirty = true;
     return LES_OK;
   }
   if (field >= LES_FIELD_BMASK1 && field <= LES_FIELD_DMASK1) {
@@ -432,6 +458,8 @@ extern "C" int les_gpu_commit_setup(les_handle *h) {
   d.logz = logz;
   d.sor_fixed = h->prm.sor_fixed;
   d.scal = h->scal_d; d.ctl = h->ctl_d; d.part = h->part_d; d.fscal = h->fscal_d;
+  d.sorA = h->sor_d[0]; d.sorB = h->sor_d[1]; d.sorR = h->sor_d[2];
+  d.cnt = h->cnt_d; d.sms = h->sms;
   les_step_plan_free(&h->plan);
   h->committed = true;
   return LES_OK;
@@ -538,11 +566,19 @@ extern "C" int les_gpu_press(les_handle *h, int n, int nmax) {
   les_launch_rhs_mean(h->dom, c);
   les_launch_sor_simple(h->dom, h->prm.nmaxp, c);
   les_launch_pav_adjust(h->dom, c);
+  h->p_dirty = false;
   return check_launch(h, "press");
 }
 
 extern "C" int les_gpu_step(les_handle *h, int n, int nmax) {
   NEED_COMMIT(h);
+  if (h->p_dirty) {
+    // p was uploaded: run this step through the per-subroutine kernels, which read p's
+    // halos exactly as stored; press leaves them consistent for the fused graph
+    les_step_enqueue(h->dom, h->prm, 0, nullptr, n, ctx_of(h));
+    h->p_dirty = false;
+    return check_launch(h, "step");
+  }
   int rc = les_step_run(h->dom, h->prm, &h->plan, n, nmax, ctx_of(h));
   if (rc) return fail(h, LES_ERR_CUDA, std::string("step: ") + cudaGetErrorString(cudaGetLastError()));
   return check_launch(h, "step");
@@ -614,9 +650,10 @@ extern "C" int les_gpu_profile(les_handle *h, int what, int reps, double *ms_avg
   CK(h, cudaEventCreate(&b));
   LesCtx c = ctx_of(h);
   CK(h, cudaEventRecord(a, h->s));
+  int per_rep = 1;  // SOR: iterations per repetition, so the result is per iteration
   for (int r = 0; r < reps; ++r) {
     switch (what) {
-      case LES_PROF_SOR: les_step_sor_pass(h->dom, h->prm, &h->plan, c); break;
+      case LES_PROF_SOR: per_rep = les_step_sor_pass(h->dom, h->prm, &h->plan, c); break;
       case LES_PROF_VELFG: les_step_velfg_pass(h->dom, c); break;
       case LES_PROF_LES: les_step_les_pass(h->dom, c); break;
       case LES_PROF_VELNW: les_launch_velnw(h->dom, c); break;
@@ -634,6 +671,6 @@ extern "C" int les_gpu_profile(les_handle *h, int what, int reps, double *ms_avg
   CK(h, cudaEventElapsedTime(&ms, a, b));
   cudaEventDestroy(a);
   cudaEventDestroy(b);
-  *ms_avg = (double)ms / reps;
+  *ms_avg = (double)ms / reps / per_rep;
   return check_launch(h, "profile");
 }

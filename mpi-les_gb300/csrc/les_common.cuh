@@ -42,6 +42,7 @@ enum {
 enum {
   CT_CONVERGED = 0,  // SOR converged flag of the current press call
   CT_ITERS,          // SOR iterations run in the current press call
+  CT_ERROR,          // set by a kernel whose bounded wait gave up (never expected)
   CT_COUNT = 4
 };
 
@@ -60,6 +61,10 @@ struct LesDom {
   int *ctl;        // CT_* slots
   double *part;    // per-block partial sums
   float *fscal;    // float copies of uout/rhsav/pav for kernels
+  float *sorA, *sorB;  // ping-pong p buffers of the fused SOR sweep (with periodic ghost rows)
+  float *sorR;         // rhs of the fused SOR sweep (with periodic ghost rows)
+  unsigned int *cnt;  // CTA completion ticket of the fused SOR sweep
+  int sms;         // SMs of the device (grid sizing)
 };
 
 __host__ __device__ __forceinline__ int lix(const LesDom &d, int i, int j, int k) {

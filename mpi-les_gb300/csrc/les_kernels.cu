@@ -371,7 +371,9 @@ __global__ void k_bondfg(LesDom d) {
 
 // ------------------------------------------------------------------ press.f95:49-60
 // rhs, plus the FP64 block partials of sum(dx1*dy1*dzn*rhs) (press.f95:63-72)
-__global__ void __launch_bounds__(BX *BY) k_rhs(LesDom d) {
+// dst: the rhs array (rhs = d.rhs) or the SOR's internal rhs buffer, which also takes
+// periodic ghost copies of rows 1, 2, jm-1, jm in rows jm+1, jm+2, -1, 0.
+__global__ void __launch_bounds__(BX *BY) k_rhs(LesDom d, float *dst, int ghost) {
   __shared__ double sh[32];
   const int i = blockIdx.x * BX + threadIdx.x + 1;
   const int j = blockIdx.y * BY + threadIdx.y + 1;
@@ -384,7 +386,13 @@ __global__ void __launch_bounds__(BX *BY) k_rhs(LesDom d) {
                     (-d.w[c - d.np] + d.w[c]) / dzn[k];
     const float rr = (d.f[c] - d.f[c - 1]) / dx1[i] + (d.g[c] - d.g[c - d.pi]) / dy1[j] +
                      (d.h[c] - d.h[c - d.np]) / dzn[k] + r / d.dt;
-    d.rhs[c] = rr;
+    dst[c] = rr;
+    if (ghost) {
+      if (j == 1) dst[lix(d, i, d.jm + 1, k)] = rr;
+      if (j == 2) dst[lix(d, i, d.jm + 2, k)] = rr;
+      if (j == d.jm - 1) dst[lix(d, i, -1, k)] = rr;
+      if (j == d.jm) dst[lix(d, i, 0, k)] = rr;
+    }
     term = (double)(dx1[i] * dy1[j] * dzn[k] * rr);
   }
   const int tid = threadIdx.y * BX + threadIdx.x;
@@ -602,9 +610,19 @@ int les_interior_blocks(const LesDom &d) {
 
 void les_launch_rhs_mean(const LesDom &d, LesCtx ctx) {
   const int nb = les_interior_blocks(d);
-  LAUNCH(ctx, k_rhs<<<interior_grid(d, d.km), dim3(BX, BY), 0, ctx.s>>>(d));
+  LAUNCH(ctx, k_rhs<<<interior_grid(d, d.km), dim3(BX, BY), 0, ctx.s>>>(d, d.rhs, 0));
   LAUNCH(ctx, k_finish_mean<<<1, 1024, 0, ctx.s>>>(d, nb, SC_RHSAV));
   LAUNCH(ctx, k_sub_mean<<<interior_grid(d, d.km), dim3(BX, BY), 0, ctx.s>>>(d, d.rhs, SC_RHSAV));
+}
+
+void les_launch_rhs_sor(const LesDom &d, LesCtx ctx) {
+  const int nb = les_interior_blocks(d);
+  LAUNCH(ctx, k_rhs<<<interior_grid(d, d.km), dim3(BX, BY), 0, ctx.s>>>(d, d.sorR, 1));
+  LAUNCH(ctx, k_finish_mean<<<1, 1024, 0, ctx.s>>>(d, nb, SC_RHSAV));
+}
+
+void les_launch_sor_begin(const LesDom &d, LesCtx ctx) {
+  LAUNCH(ctx, k_sor_begin<<<1, 1, 0, ctx.s>>>(d));
 }
 
 void les_launch_sor_simple(const LesDom &d, int nmaxp, LesCtx ctx) {

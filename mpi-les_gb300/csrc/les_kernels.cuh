@@ -21,6 +21,8 @@ void les_launch_bondfg(const LesDom &d, LesCtx ctx);
 void les_launch_boundp1(const LesDom &d, LesCtx ctx, int obey_converged);
 void les_launch_boundp2(const LesDom &d, LesCtx ctx, int obey_converged);
 void les_launch_rhs_mean(const LesDom &d, LesCtx ctx);
+void les_launch_rhs_sor(const LesDom &d, LesCtx ctx);    // rhs into the SOR buffer (+ ghost rows) and rhsav
+void les_launch_sor_begin(const LesDom &d, LesCtx ctx);
 void les_launch_sor_simple(const LesDom &d, int nmaxp, LesCtx ctx);
 void les_launch_pav_adjust(const LesDom &d, LesCtx ctx);
 void les_launch_count_nonfinite(const LesDom &d, unsigned long long *bad, LesCtx ctx);

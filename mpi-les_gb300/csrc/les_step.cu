@@ -3,15 +3,25 @@
 // The step is the reference's subroutine sequence (main.f95:260-296).  Its launch
 // sequence is recorded into a graph the first time a step runs (one graph for n == 1,
 // which includes bondv1's initial fill, one for n > 1) and replayed afterwards, so a
-// step costs one graph launch on the host.  The SOR early exit of press.f95:119 is a
-// device-side flag: once set, the remaining SOR launches of the graph return at once.
+// step costs one graph launch on the host.  press runs its SOR as the fused red-black
+// sweep of les_sor.cu (one launch per iteration, ping-ponging p between two buffers);
+// the early exit of press.f95:119 is a device-side flag that turns the remaining
+// sweeps of the graph into no-ops.
 #include <cuda_runtime.h>
 
+#include <cstdlib>
+
+#include "les_sor.cuh"
 #include "les_step.cuh"
 
 int les_step_parts_needed(int im, int jm, int km) {
-  (void)im; (void)jm; (void)km;
-  return 0;
+  (void)km;
+  int worst = 0;
+  for (int ny = 16; ny <= 32; ny += 4) {
+    const int t = les_sor_fused_tiles(im, jm, ny);
+    worst = t > worst ? t : worst;
+  }
+  return worst + 64;
 }
 
 void les_step_plan_free(LesStepPlan *plan) {
@@ -20,10 +30,47 @@ void les_step_plan_free(LesStepPlan *plan) {
     plan->exec[q] = nullptr;
     plan->launches[q] = 0;
   }
+  plan->sor_ny = 0;
+  plan->maps.valid = 0;
 }
 
-void les_step_enqueue(const LesDom &d, const les_params &prm, int sor_depth, int n, LesCtx ctx) {
-  (void)sor_depth;
+int les_step_pick_ny(const LesDom &d) {
+  if (d.jm % 2 != 0) return 0;            // the wrapped j ring needs an even jm
+  if (d.km + 1 >= LES_SOR_KMAX) return 0;  // per-k coefficients staged in shared memory
+  if (const char *e = getenv("LES_SOR_NY")) {
+    const int v = atoi(e);
+    if (v == 16 || v == 20 || v == 24 || v == 28 || v == 32) return v;
+  }
+  return les_sor_pick_ny(d.im, d.jm, d.sms > 0 ? d.sms : 152);
+}
+
+// Iteration l reads p (l = 1) or the internal buffer iteration l-1 wrote, and writes
+// the internal buffer X(l) (X = sorB for odd l, sorA for even l) or, for the last
+// iteration, p itself.  A copy-out moves the result into p when the sweep stopped
+// early (press.f95:119) or ran a single iteration.
+static void enqueue_sor_fused(const LesDom &d, const les_params &prm, int ny, const LesSorMaps *maps, LesCtx ctx) {
+  les_launch_sor_begin(d, ctx);
+  const int nit = prm.nmaxp;
+  const int ntiles = les_sor_fused_tiles(d.im, d.jm, ny);
+  for (int l = 1; l <= nit; ++l) {
+    SorArgs a;
+    a.psrc = (l == 1) ? d.p : (((l - 1) & 1) ? d.sorB : d.sorA);
+    const bool last = (l == nit) && (nit > 1);
+    a.pdst = last ? d.p : ((l & 1) ? d.sorB : d.sorA);
+    a.ghost = last ? 0 : 1;
+    a.rhs = d.sorR;
+    a.tj = ny - 4;
+    a.ntiles = ntiles;
+    a.part = d.part;
+    a.counter = d.cnt;
+    les_launch_sor_iter(d, a, ny, maps, ctx.s);
+    ++*ctx.nlaunch;
+  }
+  les_launch_sor_copyout(d, nit, ctx.s);
+  ++*ctx.nlaunch;
+}
+
+void les_step_enqueue(const LesDom &d, const les_params &prm, int ny, const LesSorMaps *maps, int n, LesCtx ctx) {
   les_launch_velnw(d, ctx);
   les_launch_bondv1(d, n, ctx);
   les_launch_velfg(d, ctx);
@@ -31,8 +78,13 @@ void les_step_enqueue(const LesDom &d, const les_params &prm, int sor_depth, int
   les_launch_les(d, ctx);
   les_launch_adam(d, ctx);
   les_launch_bondfg(d, ctx);
-  les_launch_rhs_mean(d, ctx);
-  les_launch_sor_simple(d, prm.nmaxp, ctx);
+  if (ny > 0) {
+    les_launch_rhs_sor(d, ctx);
+    enqueue_sor_fused(d, prm, ny, maps, ctx);
+  } else {
+    les_launch_rhs_mean(d, ctx);
+    les_launch_sor_simple(d, prm.nmaxp, ctx);
+  }
   les_launch_pav_adjust(d, ctx);
 }
 
@@ -40,12 +92,16 @@ int les_step_run(const LesDom &d, const les_params &prm, LesStepPlan *plan, int 
   (void)nmax;
   const int q = (n == 1) ? 0 : 1;
   if (!plan->exec[q]) {
+    if (plan->sor_ny == 0) {
+      plan->sor_ny = les_step_pick_ny(d);
+      if (plan->sor_ny > 0 && les_sor_make_maps(d, plan->sor_ny, &plan->maps) != 0) plan->maps.valid = 0;
+    }
     cudaGraph_t g = nullptr;
     long long cnt = 0;
     LesCtx cap{ctx.s, &cnt};
     cudaError_t e = cudaStreamBeginCapture(ctx.s, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return (int)e;
-    les_step_enqueue(d, prm, plan->sor_depth, n, cap);
+    les_step_enqueue(d, prm, plan->sor_ny, &plan->maps, n, cap);
     e = cudaStreamEndCapture(ctx.s, &g);
     if (e != cudaSuccess) return (int)e;
     e = cudaGraphInstantiate(&plan->exec[q], g, 0);
@@ -62,9 +118,21 @@ int les_step_run(const LesDom &d, const les_params &prm, LesStepPlan *plan, int 
   return 0;
 }
 
-void les_step_sor_pass(const LesDom &d, const les_params &prm, LesStepPlan *plan, LesCtx ctx) {
-  (void)prm; (void)plan;
-  les_launch_sor_simple(d, 1, ctx);
+int les_step_sor_pass(const LesDom &d, const les_params &prm, LesStepPlan *plan, LesCtx ctx) {
+  if (plan->sor_ny == 0) {
+    plan->sor_ny = les_step_pick_ny(d);
+    if (plan->sor_ny > 0 && les_sor_make_maps(d, plan->sor_ny, &plan->maps) != 0) plan->maps.valid = 0;
+  }
+  const int ny = plan->sor_ny;
+  if (ny == 0) {
+    les_launch_sor_simple(d, 1, ctx);
+    return 1;
+  }
+  // ten iterations as the step runs them: the first reads p, the last writes p
+  les_params ten = prm;
+  ten.nmaxp = 10;
+  enqueue_sor_fused(d, ten, ny, &plan->maps, ctx);
+  return 10;
 }
 void les_step_velfg_pass(const LesDom &d, LesCtx ctx) {
   les_launch_velfg(d, ctx);

@@ -34,10 +34,15 @@ def _run_pair(sc, nsteps, params, prec, **rkw):
     return gpu, orc
 
 
-def test_step_matches_stage_sequence(built_lib):
-    """The fused/graph step equals the per-subroutine entry points bit for bit."""
-    sc = scenario(48, 32, 16, seed=9)
-    params = lesgpu.Params(nmaxp=20)
+@pytest.mark.parametrize("shape,nmaxp", [((48, 32, 16), 20), ((130, 46, 12), 7), ((37, 6, 9), 9),
+                                         ((61, 21, 10), 6), ((250, 100, 20), 50), ((121, 2, 5), 3)])
+def test_step_matches_stage_sequence(built_lib, shape, nmaxp):
+    """The fused/graph step equals the per-subroutine entry points bit for bit.
+
+    Shapes cover partial SOR tiles in i and j, jm smaller than a tile, an odd jm (the
+    per-subroutine SOR path), jm = 2 and an odd iteration count (copy-back)."""
+    sc = scenario(*shape, seed=9)
+    params = lesgpu.Params(nmaxp=nmaxp)
     a = make_gpu(sc, params)
     b = make_gpu(sc, params)
     for n in range(1, 5):
@@ -46,6 +51,28 @@ def test_step_matches_stage_sequence(built_lib):
     for fid in lesgpu.STATE_FIELDS:
         x, y = a.download(fid), b.download(fid)
         assert np.array_equal(x.view(np.uint32), y.view(np.uint32)), lesgpu.FIELD_NAMES[fid]
+    da, db = a.diag(), b.diag()
+    assert da["iters"] == db["iters"] == nmaxp
+    assert abs(da["sor"] - db["sor"]) <= 1e-5 * abs(db["sor"])
+
+
+def test_step_after_uploading_state(built_lib):
+    """An uploaded p (halos not matching its interior) is handled exactly."""
+    from helpers import random_state
+    sc = scenario(64, 40, 12, seed=31)
+    params = lesgpu.Params(nmaxp=10)
+    a = make_gpu(sc, params)
+    b = make_gpu(sc, params)
+    st = random_state(sc, seed=77)
+    for fid, arr in st.items():
+        a.upload(fid, arr)
+        b.upload(fid, arr)
+    for n in range(2, 5):
+        a.step(n, 9)
+        b.velnw(); b.bondv1(n); b.velfg(); b.feedbf(); b.les(); b.adam(); b.press(n, 9)
+        for fid in lesgpu.STATE_FIELDS:
+            x, y = a.download(fid), b.download(fid)
+            assert np.array_equal(x.view(np.uint32), y.view(np.uint32)), (n, lesgpu.FIELD_NAMES[fid])
 
 
 @pytest.mark.parametrize("shape,nsteps", [((48, 32, 24), 10), ((40, 64, 20), 6)])
