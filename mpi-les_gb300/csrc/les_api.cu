@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <string>
@@ -86,7 +87,11 @@ struct les_handle {
   float *fscal_d = nullptr;
   unsigned long long *bad_d = nullptr;
   float *sor_d[3] = {};           // internal buffers of the fused SOR sweep (A, B, rhs)
-  unsigned int *cnt_d = nullptr;  // CTA ticket of the fused SOR sweep
+  float *diu_d[10] = {};          // diu1..9 stored by velfg for les ([0] unused)
+  float *rsp_d = nullptr;         // two planes: u/uspd and v/vspd at k = 1
+  unsigned int *cnt_d = nullptr;  // CTA tickets (fused SOR sweep, finish_mean)
+  int *fix_d = nullptr;           // deferred-block lists (FIX_COUNT lists of fix_len ints)
+  size_t fix_len = 0;
   int sms = 0;
   // p's i/j halos may disagree with its interior (set by an upload of p, cleared by
   // press): the next step then runs the per-subroutine kernels, exact for any state
@@ -134,7 +139,7 @@ extern "C" size_t les_domain_bytes(int im, int jm, int km) {
   const size_t pi = (size_t)pitch_for(im), nj = (size_t)jm + 4, nk = (size_t)km + 4;
   const size_t field = pi * nj * nk * sizeof(float);
   const size_t part = ((size_t)(im + 63) / 64 + 1) * ((size_t)(jm + 3) / 4 + 1) * (size_t)km * 2 * sizeof(double);
-  return (kNumFields + 3) * field + pi * nj * nk /*mask bytes*/ + part + 64 * 1024;
+  return (kNumFields + 3 + 9) * field + pi * nj * nk /*mask bytes*/ + 2 * pi * nj * sizeof(float) + part + 64 * 1024;
 }
 
 extern "C" int les_gpu_create(const les_dims *dims, const les_params *params, les_handle **out) {
@@ -179,10 +184,19 @@ extern "C" int les_gpu_create(const les_dims *dims, const les_params *params, le
     }
     cudaMemsetAsync(h->sor_d[q], 0, h->nfloat * sizeof(float), h->s);
   }
-  if (cudaMalloc(&h->cnt_d, 64) != cudaSuccess) {
+  for (int q = 1; q <= 9; ++q) {
+    if (cudaMalloc(&h->diu_d[q], h->nfloat * sizeof(float)) != cudaSuccess) {
+      (void)cudaGetLastError();
+      return cleanup(LES_ERR_NOMEM);
+    }
+    cudaMemsetAsync(h->diu_d[q], 0, h->nfloat * sizeof(float), h->s);
+  }
+  if (cudaMalloc(&h->rsp_d, 2 * (size_t)h->np * sizeof(float)) != cudaSuccess ||
+      cudaMalloc(&h->cnt_d, 64) != cudaSuccess) {
     (void)cudaGetLastError();
     return cleanup(LES_ERR_NOMEM);
   }
+  cudaMemsetAsync(h->rsp_d, 0, 2 * (size_t)h->np * sizeof(float), h->s);
   cudaMemsetAsync(h->cnt_d, 0, 64, h->s);
   cudaMemsetAsync(h->mask_d, 0, h->nfloat, h->s);
   if (cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, h->dev) != cudaSuccess) {
@@ -193,7 +207,18 @@ extern "C" int les_gpu_create(const les_dims *dims, const les_params *params, le
   // partial-sum buffer: the largest per-block count of any reduction kernel
   h->npart = (size_t)std::max<long long>(
       {(long long)((im + 63) / 64) * ((jm + 3) / 4) * km * 2 + 64, (long long)les_step_parts_needed(im, jm, km)});
-  if (cudaMalloc(&h->part_d, h->npart * sizeof(double)) != cudaSuccess ||
+  // deferred-block lists: [count, ticket, ids...] for the largest grid of those kernels
+  {
+    const long long fused = (long long)((im + 31) / 32) * ((jm + 1) / 2) * ((km + 3) / 4);
+    const long long inter = (long long)((im + 63) / 64) * ((jm + 3) / 4) * km;
+    h->fix_len = 2 + (size_t)std::max(fused, inter);
+  }
+  if (cudaMalloc(&h->fix_d, FIX_COUNT * h->fix_len * sizeof(int)) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return cleanup(LES_ERR_NOMEM);
+  }
+  cudaMemsetAsync(h->fix_d, 0, FIX_COUNT * h->fix_len * sizeof(int), h->s);
+  if (cudaMalloc(&h->part_d, (h->npart + 256) * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&h->scal_d, SC_COUNT * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&h->ctl_d, CT_COUNT * sizeof(int)) != cudaSuccess ||
       cudaMalloc(&h->fscal_d, SC_COUNT * sizeof(float)) != cudaSuccess ||
@@ -224,7 +249,10 @@ extern "C" int les_gpu_destroy(les_handle *h) {
   cudaFree(h->fscal_d);
   cudaFree(h->bad_d);
   for (int q = 0; q < 3; ++q) cudaFree(h->sor_d[q]);
+  for (int q = 1; q <= 9; ++q) cudaFree(h->diu_d[q]);
+  cudaFree(h->rsp_d);
   cudaFree(h->cnt_d);
+  cudaFree(h->fix_d);
   if (h->s) cudaStreamDestroy(h->s);
   (void)cudaGetLastError();
   delete h;
@@ -389,7 +417,18 @@ extern "C" int les_gpu_commit_setup(les_handle *h) {
           if (memcmp(&f, &g, 4) != 0) { need_cn1 = true; break; }
         }
   }
-  // 1-D device buffer: [dx1 dy1 dzn dzs dxs dys z2 cn2l cn2s cn3l cn3s cn4l cn4s delx1 ca cb cc ck]
+  // correctly rounded reciprocals of the spacings and of neighbour sums (dvs, dvz)
+  std::vector<float> rx1(im + 3), rx1s(im + 2), rxs(im + 1), ry1(jm + 2), ry1s(jm + 1), rys(jm + 1);
+  std::vector<float> rzn(km + 4), rzs(km + 4), rzsum(km + 3);
+  for (int i = -1; i <= im + 1; ++i) rx1[i + 1] = 1.f / dx1(i);
+  for (int i = -1; i <= im; ++i) rx1s[i + 1] = 1.f / (dx1(i) + dx1(i + 1));
+  for (int i = 0; i <= im; ++i) rxs[i] = 1.f / dxs(i);
+  for (int j = 0; j <= jm + 1; ++j) ry1[j] = 1.f / dy1(j);
+  for (int j = 0; j <= jm; ++j) { ry1s[j] = 1.f / (dy1(j) + dy1(j + 1)); rys[j] = 1.f / dys(j); }
+  for (int k = -1; k <= km + 2; ++k) { rzn[k + 1] = 1.f / dzn(k); rzs[k + 1] = 1.f / dzs(k); }
+  for (int k = -1; k <= km + 1; ++k) rzsum[k + 1] = 1.f / (dzn(k) + dzn(k + 1));
+  // 1-D device buffer: [dx1 dy1 dzn dzs dxs dys z2 cn2l cn2s cn3l cn3s cn4l cn4s delx1 ca cb cc ck
+  //                     and the reciprocals]
   struct Seg { int id; int lo; int n; const float *src; };
   std::vector<float> z2v(km + 3, 0.f);
   if (h->h1d.count(LES_FIELD_Z2)) z2v = h->h1d[LES_FIELD_Z2];
@@ -402,7 +441,10 @@ extern "C" int les_gpu_commit_setup(les_handle *h) {
       {LES_FIELD_CN3L, 1, jm, h->h1d[LES_FIELD_CN3L].data()},    {LES_FIELD_CN3S, 1, jm, h->h1d[LES_FIELD_CN3S].data()},
       {LES_FIELD_CN4L, 1, km, h->h1d[LES_FIELD_CN4L].data()},    {LES_FIELD_CN4S, 1, km, h->h1d[LES_FIELD_CN4S].data()},
       {LES_FIELD_DELX1, 1, km, h->h1d[LES_FIELD_DELX1].data()},
-      {-1, 0, im + 1, ca.data()}, {-2, 0, jm + 1, cb.data()}, {-3, 0, km + 1, cc.data()}, {-4, 0, km + 1, ck.data()}};
+      {-1, 0, im + 1, ca.data()}, {-2, 0, jm + 1, cb.data()}, {-3, 0, km + 1, cc.data()}, {-4, 0, km + 1, ck.data()},
+      {-5, -1, km + 4, rzn.data()}, {-6, -1, km + 4, rzs.data()}, {-7, -1, km + 3, rzsum.data()},
+      {-8, -1, im + 3, rx1.data()}, {-9, -1, im + 2, rx1s.data()}, {-10, 0, im + 1, rxs.data()},
+      {-11, 0, jm + 2, ry1.data()}, {-12, 0, jm + 1, ry1s.data()}, {-13, 0, jm + 1, rys.data()}};
   size_t total = 0;
   std::vector<size_t> off(segs.size());
   for (size_t q = 0; q < segs.size(); ++q) { off[q] = total; total += (segs[q].n + 7) / 8 * 8; }
@@ -417,6 +459,8 @@ extern "C" int les_gpu_commit_setup(les_handle *h) {
   g.dx1 = P(0); g.dy1 = P(1); g.dzn = P(2); g.dzs = P(3); g.dxs = P(4); g.dys = P(5); g.z2 = P(6);
   g.cn2l = P(7); g.cn2s = P(8); g.cn3l = P(9); g.cn3s = P(10); g.cn4l = P(11); g.cn4s = P(12); g.delx1 = P(13);
   g.cn1a = P(14); g.cn1b = P(15); g.cn1c = P(16); g.cn1k = uniform ? P(17) : nullptr;
+  g.rdzn = P(18); g.rdzs = P(19); g.rdzsum = P(20);
+  g.rdx1 = P(21); g.rdx1s = P(22); g.rdxs = P(23); g.rdy1 = P(24); g.rdy1s = P(25); g.rdys = P(26);
   // full cn1 only if the uploaded one is not the separable formula bit for bit
   cudaFree(h->cn1_d); h->cn1_d = nullptr;
   if (need_cn1) {
@@ -459,7 +503,33 @@ extern "C" int les_gpu_commit_setup(les_handle *h) {
   d.sor_fixed = h->prm.sor_fixed;
   d.scal = h->scal_d; d.ctl = h->ctl_d; d.part = h->part_d; d.fscal = h->fscal_d;
   d.sorA = h->sor_d[0]; d.sorB = h->sor_d[1]; d.sorR = h->sor_d[2];
+  {  // power-of-two x/y spacings: exact reciprocal multiplications (dvs)
+    auto pow2 = [](float x) { int e; return x > 0.f && std::isfinite(x) && std::frexp(x, &e) == 0.5f; };
+    const float P = dx1(1), Q = dy1(1);
+    bool ok = pow2(P) && pow2(Q);
+    for (int i = -1; i <= im + 1 && ok; ++i) ok = (dx1(i) == P);
+    for (int i = 0; i <= im && ok; ++i) ok = (dxs(i) == P);
+    for (int j = 0; j <= jm + 1 && ok; ++j) ok = (dy1(j) == Q);
+    for (int j = 0; j <= jm && ok; ++j) ok = (dys(j) == Q);
+    d.xy_pow2 = ok ? 1 : 0;
+  }
+  {  // every divisor in [2^-20, 2^20]: reciprocal-corrected divisions (dvz)
+    auto inr = [](float x) { const float a = std::fabs(x); return std::isfinite(x) && a >= 0x1p-20f && a <= 0x1p20f; };
+    bool ok = inr(logz) && inr(h->prm.ro) && inr(h->prm.dt);
+    for (int i = -1; i <= im + 1 && ok; ++i) ok = inr(dx1(i)) && (i > im || inr(dx1(i) + dx1(i + 1)));
+    for (int i = 0; i <= im && ok; ++i) ok = inr(dxs(i));
+    for (int j = 0; j <= jm + 1 && ok; ++j) ok = inr(dy1(j)) && (j > jm || (inr(dy1(j) + dy1(j + 1)) && inr(dys(j))));
+    for (int k = -1; k <= km + 2 && ok; ++k) ok = inr(dzn(k)) && inr(dzs(k));
+    for (int k = -1; k <= km + 1 && ok; ++k) ok = inr(dzn(k) + dzn(k + 1));
+    d.zfast = ok ? 1 : 0;
+    if (getenv("LES_IEEE_DIV")) d.xy_pow2 = d.zfast = 0;  // every division an IEEE division (tests)
+    d.rro = 1.f / h->prm.ro; d.rdt = 1.f / h->prm.dt; d.rlogz = 1.f / logz;
+  }
   d.cnt = h->cnt_d; d.sms = h->sms;
+  d.part2 = h->part_d + h->npart;
+  for (int q = 0; q < FIX_COUNT; ++q) d.fix[q] = h->fix_d + q * h->fix_len;
+  for (int q = 0; q <= 9; ++q) d.diu[q] = h->diu_d[q];
+  d.ruspd = h->rsp_d; d.rvspd = h->rsp_d + h->np;
   les_step_plan_free(&h->plan);
   h->committed = true;
   return LES_OK;
@@ -525,7 +595,7 @@ extern "C" int les_gpu_bondv1(les_handle *h, int n) {
 }
 extern "C" int les_gpu_velfg(les_handle *h) {
   NEED_COMMIT(h);
-  les_launch_velfg(h->dom, ctx_of(h));
+  les_launch_velfg_fused(h->dom, false, ctx_of(h));
   return check_launch(h, "velfg");
 }
 extern "C" int les_gpu_feedbf(les_handle *h) {
@@ -535,7 +605,7 @@ extern "C" int les_gpu_feedbf(les_handle *h) {
 }
 extern "C" int les_gpu_les(les_handle *h) {
   NEED_COMMIT(h);
-  les_launch_les(h->dom, ctx_of(h));
+  les_launch_les_fused(h->dom, false, ctx_of(h));
   return check_launch(h, "les");
 }
 extern "C" int les_gpu_adam(les_handle *h) {

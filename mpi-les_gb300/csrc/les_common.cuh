@@ -7,13 +7,13 @@
 // row pitch pi (floats) is a multiple of 16 (64 bytes).
 //
 // Face quantities.  The reference's vel2 (src/vel2.f95:74-356) stores 27 temporary
-// arrays (nou1-9, diu1-9, cov1-9) that velFG and les then read.  Here they are never
-// stored: each kernel recomputes the value the reference array holds at the index it
-// reads, from u, v, w, with the same FP32 expression.  The halo copies of
-// vel2.f95:202-318 become index remaps (i = im+1 -> im, j = jm+1 -> 1, j = 0 -> jm)
-// and entries the reference never writes read as 0 (diu2/diu3 at i = 0, diu7/diu8 at
-// k = 0 and k >= km, diu9 at k = km+1).  Recomputation is exact: FP32 arithmetic is
-// deterministic, and the kernels are built with --fmad=false and IEEE div/sqrt.
+// arrays (nou1-9, diu1-9, cov1-9) that velFG and les then read.  Here nou and cov are
+// never stored (velfg forms them where it needs them) and only diu1-9 are: les reads
+// them back.  The halo copies of vel2.f95:202-318 become index remaps (i = im+1 -> im,
+// j = jm+1 -> 1, j = 0 -> jm) and entries the reference never writes read as 0
+// (diu2/diu3 at i = 0, diu7/diu8 at k = 0 and k >= km, diu9 at k = km+1).  The FP32
+// arithmetic is the reference's, operation for operation: the kernels are built with
+// --fmad=false, and every division gives the IEEE quotient (dvz, dvs below).
 #pragma once
 #include <cstdint>
 
@@ -27,6 +27,10 @@ struct LesGrid1 {
   const float *cn2l, *cn2s, *cn3l, *cn3s, *cn4l, *cn4s, *delx1;
   const float *cn1a, *cn1b, *cn1c;  // 2/(dxs(i-1)dxs(i)), 2/(dys(j-1)dys(j)), 2/(dzs(k-1)dzs(k))
   const float *cn1k;                // 1/((a+b)+c) when a and b are the same for all i, j
+  // correctly rounded FP32 reciprocals of the spacings and of the neighbour sums:
+  // 1/dx1(i), 1/(dx1(i)+dx1(i+1)), 1/dxs(i), the same in y, 1/dzn(k), 1/dzs(k),
+  // 1/(dzn(k)+dzn(k+1)), indexed like the spacing arrays
+  const float *rdx1, *rdx1s, *rdxs, *rdy1, *rdy1s, *rdys, *rdzn, *rdzs, *rdzsum;
 };
 
 // Device scalar slots (double) of a domain.
@@ -46,6 +50,9 @@ enum {
   CT_COUNT = 4
 };
 
+// deferred-block lists, one per kernel that divides with dvz
+enum { FIX_VELNW = 0, FIX_VELFG, FIX_VISC, FIX_RHS, FIX_COUNT };
+
 struct LesDom {
   int im, jm, km;
   int pi, nj, np;  // row pitch (floats), rows per plane, floats per plane
@@ -63,8 +70,23 @@ struct LesDom {
   float *fscal;    // float copies of uout/rhsav/pav for kernels
   float *sorA, *sorB;  // ping-pong p buffers of the fused SOR sweep (with periodic ghost rows)
   float *sorR;         // rhs of the fused SOR sweep (with periodic ghost rows)
-  unsigned int *cnt;  // CTA completion ticket of the fused SOR sweep
+  unsigned int *cnt;  // CTA completion tickets: [0] fused SOR sweep, [8] finish_mean
+  double *part2;      // second-level partial sums of finish_mean (FIN_BLOCKS)
   int sms;         // SMs of the device (grid sizing)
+  // xy_pow2: every x and y spacing is the same power of two (dvs multiplies);
+  // zfast: every spacing, spacing sum and scalar divisor lies in [2^-20, 2^20] (dvz),
+  // with the reciprocals of ro, dt and logz
+  int xy_pow2;
+  int zfast;
+  float rro, rdt, rlogz;
+  // deferred-block lists of the kernels that use dvz (FIX_*): [0] count, [1] ticket of
+  // the fixup kernel, then the linear ids of the blocks left to the fixup kernel
+  int *fix[4];
+  // diu1..9 as velfg computed them (vel2.f95:74-197), interior cells (plus plane km+1
+  // of diu3/diu6), read by les the way les.f95 reads the reference's arrays; and the
+  // wall-function ratios u(i,j,1)/uspd, v(i,j,1)/vspd of vel2.f95:351-356 (one plane)
+  float *diu[10];
+  float *ruspd, *rvspd;
 };
 
 __host__ __device__ __forceinline__ int lix(const LesDom &d, int i, int j, int k) {
@@ -96,146 +118,90 @@ __device__ __forceinline__ float vspd_raw(const LesDom &d, int i, int j) {
                   (dy1[j] + dy1[j + 1]);
   return pow_half(a * a + b * b);
 }
-// log-law wall gradients diu3(i,j,1), diu6(i,j,1) (vel2.f95:138,173)
+// a / b for a divisor b fixed at set-up, with y = RN(1/b) computed on the host.
+// ZF: Markstein's corrected quotient q0 = a*y, r = a - b*q0 (exact by FMA), q = q0 + r*y
+// (P. Markstein, IBM J. Res. Dev. 34(1), 1990: with y the correctly rounded reciprocal,
+// q is the correctly rounded a/b while r and q stay normal).  That holds for
+// |b| in [2^-20, 2^20] (checked at set-up) and |a| in [2^-100, 2^100]; a zero dividend
+// is exact as a*y (sign included).  Any other dividend (tiny, huge, inf, NaN) sets
+// `bad` and the caller recomputes its cell with IEEE divisions.  The path is free of
+// branches and calls, so a kernel can issue its whole stencil's loads up front.
+// !ZF: the IEEE division.
+template <bool ZF>
+__device__ __forceinline__ float dvz(float a, float b, float y, unsigned &bad) {
+  if (!ZF) return a / b;
+  const float aa = fabsf(a);
+  const float q0 = __fmul_rn(a, y);
+  const float r = __fmaf_rn(-q0, b, a);
+  const float q1 = __fmaf_rn(r, y, q0);
+  bad |= (unsigned)(!(aa >= 0x1p-100f && aa <= 0x1p100f) && aa != 0.f);
+  return aa == 0.f ? q0 : q1;
+}
+// x / (an x or y spacing, or the sum of two): P2 (all x and y spacings the same power
+// of two) makes it a multiplication by the exact reciprocal -- both round the same
+// real number -- else as dvz
+template <bool P2, bool ZF>
+__device__ __forceinline__ float dvs(float x, float den, float rden, unsigned &bad) {
+  return P2 ? x * rden : dvz<ZF>(x, den, rden, bad);
+}
+
+// Block-level deferral.  A block in which some thread met a dividend outside dvz's range
+// stores nothing; thread 0 appends the block's linear id to `list`, and a fixup kernel
+// launched next recomputes the listed blocks with IEEE divisions.  The hot kernels thus
+// hold no IEEE division code at all, whose presence alone (even never executed) slows
+// their memory pipeline several-fold.  Every thread of the block must call this.
+__device__ __forceinline__ bool defer_block(unsigned bad, int *list) {
+  if (!__syncthreads_or(bad)) return false;
+  if (threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0) {
+    const int s = atomicAdd(list, 1);
+    list[2 + s] = (int)((blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x);
+  }
+  return true;
+}
+// The fixup side: body(bx, by, bz) for every listed block of a main grid g, then the
+// last CTA to finish resets the list for the next launch.
+template <class F>
+__device__ __forceinline__ void for_deferred(int *list, uint3 g, F body) {
+  const int n = *(volatile int *)list;
+  for (int q = blockIdx.x; q < n; q += gridDim.x) {
+    const int id = list[2 + q];
+    body((int)(id % g.x), (int)((id / g.x) % g.y), (int)(id / (g.x * g.y)));
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0) {
+    __threadfence();
+    if (atomicAdd(list + 1, 1) == (int)gridDim.x - 1) {
+      list[0] = 0;
+      list[1] = 0;
+    }
+  }
+}
+
+// log-law wall gradients diu3(i,j,1), diu6(i,j,1) (vel2.f95:138,173), IEEE divisions
 __device__ __forceinline__ float wall_grad(const LesDom &d, float spd, float vel) {
   const float hz = 0.5f * d.gr.dzn[1];
   return spd * 0.4f / d.logz / hz / 0.4f * vel / spd;
 }
 
-// ---- diu1..9 as the reference arrays hold them after vel2 (read ranges of les) --
-__device__ __forceinline__ float diu1(const LesDom &d, int i, int j, int k) {
-  const int ii = min(i, d.im);
-  return (-U_(ii - 1, j, k) + U_(ii, j, k)) / d.gr.dx1[ii];
+// Knuth's TwoSum: s = fl(a + b) and e with s + e == a + b exactly (the kernels are
+// built with --fmad=false, so nothing here is contracted).
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
 }
-__device__ __forceinline__ float diu2(const LesDom &d, int i, int j, int k) {
-  if (i <= 0) return 0.f;
-  const int jj = (j > d.jm) ? 1 : j;
-  return 2.f * (-U_(i, jj - 1, k) + U_(i, jj, k)) / (d.gr.dy1[jj - 1] + d.gr.dy1[jj]);
-}
-__device__ __forceinline__ float diu3(const LesDom &d, int i, int j, int k) {
-  if (i <= 0) return 0.f;
-  if (k == 1) return wall_grad(d, uspd_raw(d, i, j), U_(i, j, 1));
-  return (-U_(i, j, k - 1) + U_(i, j, k)) / d.gr.dzs[k - 1];
-}
-__device__ __forceinline__ float diu4(const LesDom &d, int i, int j, int k) {
-  const int ii = min(i, d.im);
-  const int jj = (j <= 0) ? d.jm : j;
-  return 2.f * (-V_(ii - 1, jj, k) + V_(ii, jj, k)) / (d.gr.dx1[ii - 1] + d.gr.dx1[ii]);
-}
-__device__ __forceinline__ float diu5(const LesDom &d, int i, int j, int k) {
-  const int jj = (j > d.jm) ? 1 : j;
-  return (-V_(i, jj - 1, k) + V_(i, jj, k)) / d.gr.dy1[jj];
-}
-__device__ __forceinline__ float diu6(const LesDom &d, int i, int j, int k) {
-  const int jj = (j <= 0) ? d.jm : j;
-  if (k == 1) return wall_grad(d, vspd_raw(d, i, jj), V_(i, jj, 1));
-  return (-V_(i, jj, k - 1) + V_(i, jj, k)) / d.gr.dzs[k - 1];
-}
-__device__ __forceinline__ float diu7(const LesDom &d, int i, int j, int k) {
-  if (k <= 0 || k >= d.km) return 0.f;
-  const int ii = min(i, d.im);
-  return 2.f * (-W_(ii - 1, j, k) + W_(ii, j, k)) / (d.gr.dx1[ii - 1] + d.gr.dx1[ii]);
-}
-__device__ __forceinline__ float diu8(const LesDom &d, int i, int j, int k) {
-  if (k <= 0 || k >= d.km) return 0.f;
-  const int jj = (j > d.jm) ? 1 : j;
-  return 2.f * (-W_(i, jj - 1, k) + W_(i, jj, k)) / (d.gr.dy1[jj - 1] + d.gr.dy1[jj]);
-}
-__device__ __forceinline__ float diu9(const LesDom &d, int i, int j, int k) {
-  if (k > d.km) return 0.f;
-  return (-W_(i, j, k - 1) + W_(i, j, k)) / d.gr.dzn[k];
-}
-
-// ---- cov1..9 = nou*diu as read by velFG (velFG.f95:64-110) --------------------
-__device__ __forceinline__ float cov1(const LesDom &d, int i, int j, int k) {
-  const int ii = min(i, d.im);
-  const float a = U_(ii - 1, j, k), b = U_(ii, j, k);
-  return ((a + b) / 2.f) * ((-a + b) / d.gr.dx1[ii]);
-}
-__device__ __forceinline__ float cov2(const LesDom &d, int i, int j, int k) {
-  const int jj = (j > d.jm) ? 1 : j;
-  const float *dx1 = d.gr.dx1, *dy1 = d.gr.dy1;
-  const float nou = (dx1[i + 1] * V_(i, jj - 1, k) + dx1[i] * V_(i + 1, jj - 1, k)) / (dx1[i] + dx1[i + 1]);
-  const float diu = 2.f * (-U_(i, jj - 1, k) + U_(i, jj, k)) / (dy1[jj - 1] + dy1[jj]);
-  return nou * diu;
-}
-__device__ __forceinline__ float cov3(const LesDom &d, int i, int j, int k) {
-  const float *dx1 = d.gr.dx1;
-  if (k == 1) {
-    const float nou = 0.5f * (dx1[i + 1] * W_(i, j, 1) + dx1[i] * W_(i + 1, j, 1)) / (dx1[i] + dx1[i + 1]);
-    return nou * wall_grad(d, uspd_raw(d, i, j), U_(i, j, 1));
+// Sum of one FP32 term per lane, returned in FP64 on lane 0.  The warp tree carries an
+// unevaluated pair (hi, lo): hi adds by TwoSum, lo gathers the rounding errors, so the
+// FP64 pipe (slow on this part) is touched once per warp, not once per term.  The
+// error stays near 2^-47 of the sum of magnitudes; the order is fixed (deterministic).
+__device__ __forceinline__ double warp_sum_pair(float x) {
+  float hi = x, lo = 0.f;
+  for (int o = 16; o > 0; o >>= 1) {
+    const float h2 = __shfl_down_sync(0xffffffffu, hi, o), l2 = __shfl_down_sync(0xffffffffu, lo, o);
+    float s, e;
+    two_sum(hi, h2, s, e);
+    hi = s;
+    lo = (lo + l2) + e;
   }
-  const float nou = (dx1[i + 1] * W_(i, j, k - 1) + dx1[i] * W_(i + 1, j, k - 1)) / (dx1[i] + dx1[i + 1]);
-  const float diu = (-U_(i, j, k - 1) + U_(i, j, k)) / d.gr.dzs[k - 1];
-  return nou * diu;
-}
-__device__ __forceinline__ float cov4(const LesDom &d, int i, int j, int k) {
-  const int ii = min(i, d.im);
-  const float *dx1 = d.gr.dx1, *dy1 = d.gr.dy1;
-  const float nou = (dy1[j + 1] * U_(ii - 1, j, k) + dy1[j] * U_(ii - 1, j + 1, k)) / (dy1[j] + dy1[j + 1]);
-  const float diu = 2.f * (-V_(ii - 1, j, k) + V_(ii, j, k)) / (dx1[ii - 1] + dx1[ii]);
-  return (nou - 0.f) * diu;
-}
-__device__ __forceinline__ float cov5(const LesDom &d, int i, int j, int k) {
-  const int jj = (j > d.jm) ? 1 : j;
-  const float a = V_(i, jj - 1, k), b = V_(i, jj, k);
-  return ((a + b) / 2.f) * ((-a + b) / d.gr.dy1[jj]);
-}
-__device__ __forceinline__ float cov6(const LesDom &d, int i, int j, int k) {
-  const float *dy1 = d.gr.dy1;
-  if (k == 1) {
-    const float nou = 0.5f * (dy1[j + 1] * W_(i, j, 1) + dy1[j] * W_(i, j + 1, 1)) / (dy1[j] + dy1[j + 1]);
-    return nou * wall_grad(d, vspd_raw(d, i, j), V_(i, j, 1));
-  }
-  const float nou = (dy1[j + 1] * W_(i, j, k - 1) + dy1[j] * W_(i, j + 1, k - 1)) / (dy1[j] + dy1[j + 1]);
-  const float diu = (-V_(i, j, k - 1) + V_(i, j, k)) / d.gr.dzs[k - 1];
-  return nou * diu;
-}
-__device__ __forceinline__ float cov7(const LesDom &d, int i, int j, int k) {
-  const int ii = min(i, d.im);
-  const float *dx1 = d.gr.dx1, *dzn = d.gr.dzn;
-  const float nou = (dzn[k + 1] * U_(ii - 1, j, k) + dzn[k] * U_(ii - 1, j, k + 1)) / (dzn[k] + dzn[k + 1]);
-  const float diu = 2.f * (-W_(ii - 1, j, k) + W_(ii, j, k)) / (dx1[ii - 1] + dx1[ii]);
-  return (nou - 0.f) * diu;
-}
-__device__ __forceinline__ float cov8(const LesDom &d, int i, int j, int k) {
-  const int jj = (j > d.jm) ? 1 : j;
-  const float *dy1 = d.gr.dy1, *dzn = d.gr.dzn;
-  const float nou = (dzn[k + 1] * V_(i, jj - 1, k) + dzn[k] * V_(i, jj - 1, k + 1)) / (dzn[k] + dzn[k + 1]);
-  const float diu = 2.f * (-W_(i, jj - 1, k) + W_(i, jj, k)) / (dy1[jj - 1] + dy1[jj]);
-  return nou * diu;
-}
-__device__ __forceinline__ float cov9(const LesDom &d, int i, int j, int k) {
-  const float a = W_(i, j, k - 1), b = W_(i, j, k);
-  return ((a + b) / 2.f) * ((-a + b) / d.gr.dzn[k]);
-}
-
-// Warp-level FP32 sum followed by an FP64 block sum: one double per block.  FP32
-// inside a warp keeps the (slow on this part) FP64 pipe out of the per-cell path.
-template <int NT>
-__device__ __forceinline__ double block_sum_f32_to_f64(float x, double *sh) {
-  for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  if (lane == 0) sh[wid] = (double)x;
-  __syncthreads();
-  double s = 0.0;
-  if (threadIdx.x == 0) {
-    for (int q = 0; q < NT / 32; ++q) s += sh[q];
-  }
-  __syncthreads();
-  return s;
-}
-// FP64 block sum of per-thread FP64 values (used where each term must enter in FP64).
-template <int NT>
-__device__ __forceinline__ double block_sum_f64(double x, double *sh) {
-  for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  if (lane == 0) sh[wid] = x;
-  __syncthreads();
-  double s = 0.0;
-  if (threadIdx.x == 0) {
-    for (int q = 0; q < NT / 32; ++q) s += sh[q];
-  }
-  __syncthreads();
-  return s;
+  return (double)hi + (double)lo;
 }

@@ -2,8 +2,8 @@
 //
 // One kernel (or a short fixed sequence of small kernels) per reference subroutine,
 // each a drop-in for that subroutine on device-resident state.  These are the
-// building blocks behind the per-subroutine C-ABI entry points; the whole-step path
-// uses the fused kernels of les_fused.cu and les_sor.cu instead.
+// building blocks behind the per-subroutine C-ABI entry points.  velfg and les live in
+// les_fused.cu (shared with the whole step); the whole step's SOR is les_sor.cu.
 //
 // Exactness: every interior update is an independent function of values no other
 // thread of the same launch writes, so a one-thread-per-cell launch reproduces the
@@ -12,6 +12,8 @@
 // residual) are per-domain deterministic reductions: FP64 where the reference sums
 // many FP32 terms.
 #include <cuda_runtime.h>
+
+#include <algorithm>
 
 #include "les_common.cuh"
 #include "les_kernels.cuh"
@@ -31,18 +33,45 @@ inline dim3 interior_grid(const LesDom &d, int kn) {
   if (i > d.im || j > d.jm) return;
 
 // ------------------------------------------------------------------ velnw.f95:27-59
-__global__ void __launch_bounds__(BX *BY) k_velnw(LesDom d) {
-  INTERIOR_IJK
-  const int c = lix(d, i, j, k);
-  const float pc = d.p[c];
-  float pz = (-pc + d.p[c + 1]) / d.ro / d.gr.dxs[i];
-  d.u[c] = d.u[c] + d.dt * (d.f[c] - pz);
-  pz = (-pc + d.p[c + d.pi]) / d.ro / d.gr.dys[j];
-  d.v[c] = d.v[c] + d.dt * (d.g[c] - pz);
+// new u, v, w of one cell; P2 / ZF: division forms of dvs / dvz (les_common.cuh)
+// (p, f, g, h are only read here: read-only loads)
+template <bool P2, bool ZF>
+__device__ __forceinline__ void velnw_cell(const LesDom &d, int i, int j, int k, int c, float &un, float &vn, float &wn,
+                                           unsigned &bd) {
+  const float pc = __ldg(d.p + c);
+  float pz = dvs<P2, ZF>(dvz<ZF>(-pc + __ldg(d.p + c + 1), d.ro, d.rro, bd), d.gr.dxs[i], d.gr.rdxs[i], bd);
+  un = d.u[c] + d.dt * (__ldg(d.f + c) - pz);
+  pz = dvs<P2, ZF>(dvz<ZF>(-pc + __ldg(d.p + c + d.pi), d.ro, d.rro, bd), d.gr.dys[j], d.gr.rdys[j], bd);
+  vn = d.v[c] + d.dt * (__ldg(d.g + c) - pz);
   if (k <= d.km - 1) {
-    pz = (-pc + d.p[c + d.np]) / d.ro / d.gr.dzs[k];
-    d.w[c] = d.w[c] + d.dt * (d.h[c] - pz);
+    pz = dvz<ZF>(dvz<ZF>(-pc + __ldg(d.p + c + d.np), d.ro, d.rro, bd), d.gr.dzs[k], d.gr.rdzs[k], bd);
+    wn = d.w[c] + d.dt * (__ldg(d.h + c) - pz);
   }
+}
+// velnw of the block (bx, by, bz); ZF: reciprocal-corrected divisions with blocks that
+// meet a dividend outside their range deferred to k_velnw_fix (les_common.cuh)
+template <bool P2, bool ZF>
+__device__ __forceinline__ void velnw_block(const LesDom &d, int bx, int by, int bz) {
+  const int i0 = bx * BX + threadIdx.x + 1, j0 = by * BY + threadIdx.y + 1, k = bz + 1;
+  const bool in = (i0 <= d.im && j0 <= d.jm);
+  const int i = min(i0, d.im), j = min(j0, d.jm);  // past the edge: the edge cell again, not stored
+  const int c = lix(d, i, j, k);
+  float un = 0.f, vn = 0.f, wn = 0.f;
+  unsigned bd = 0;
+  velnw_cell<P2, ZF>(d, i, j, k, c, un, vn, wn, bd);
+  if (ZF && defer_block(bd, d.fix[FIX_VELNW])) return;
+  if (!in) return;
+  d.u[c] = un;
+  d.v[c] = vn;
+  if (k <= d.km - 1) d.w[c] = wn;
+}
+template <bool P2, bool ZF>
+__global__ void __launch_bounds__(BX *BY) k_velnw(LesDom d) {
+  velnw_block<P2, ZF>(d, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+template <bool P2>
+__global__ void __launch_bounds__(BX *BY) k_velnw_fix(LesDom d, uint3 g) {
+  for_deferred(d.fix[FIX_VELNW], g, [&](int bx, int by, int bz) { velnw_block<P2, false>(d, bx, by, bz); });
 }
 
 // ------------------------------------------------------------------ bondv1.f95
@@ -128,46 +157,6 @@ __global__ void k_bondv1_topbottom(LesDom d) {
   d.w[lix(d, i, j, d.km)] = 0.f;
 }
 
-// ------------------------------------------------------------------ velFG.f95:64-110
-__global__ void __launch_bounds__(BX *BY) k_velfg(LesDom d) {
-  INTERIOR_IJK
-  const float *dx1 = d.gr.dx1, *dy1 = d.gr.dy1, *dzn = d.gr.dzn, *dzs = d.gr.dzs;
-  const int c = lix(d, i, j, k);
-  {  // u
-    const float covx1 = (dx1[i + 1] * cov1(d, i, j, k) + dx1[i] * cov1(d, i + 1, j, k)) / (dx1[i] + dx1[i + 1]);
-    const float covy1 = (cov2(d, i, j, k) + cov2(d, i, j + 1, k)) / 2.f;
-    const float covz1 = (cov3(d, i, j, k) + cov3(d, i, j, k + 1)) / 2.f;
-    const float covc = covx1 + covy1 + covz1;
-    const float dfu1 = 2.f * (-diu1(d, i, j, k) + diu1(d, i + 1, j, k)) / (dx1[i] + dx1[i + 1]) +
-                       (-diu2(d, i, j, k) + diu2(d, i, j + 1, k)) / dy1[j] +
-                       (-diu3(d, i, j, k) + diu3(d, i, j, k + 1)) / dzn[k];
-    const float df = d.vn * dfu1;
-    d.f[c] = (-covc + df);
-  }
-  {  // v
-    const float covx1 = (cov4(d, i, j, k) + cov4(d, i + 1, j, k)) / 2.f;
-    const float covy1 = (dy1[j + 1] * cov5(d, i, j, k) + dy1[j] * cov5(d, i, j + 1, k)) / (dy1[j] + dy1[j + 1]);
-    const float covz1 = (cov6(d, i, j, k) + cov6(d, i, j, k + 1)) / 2.f;
-    const float covc = covx1 + covy1 + covz1;
-    const float dfv1 = (-diu4(d, i, j, k) + diu4(d, i + 1, j, k)) / dx1[i] +
-                       2.f * (-diu5(d, i, j, k) + diu5(d, i, j + 1, k)) / (dy1[j] + dy1[j + 1]) +
-                       (-diu6(d, i, j, k) + diu6(d, i, j, k + 1)) / dzn[k];
-    const float df = d.vn * dfv1;
-    d.g[c] = (-covc + df);
-  }
-  if (k <= d.km - 1) {  // w
-    const float covx1 = (cov7(d, i, j, k) + cov7(d, i + 1, j, k)) / 2.f;
-    const float covy1 = (cov8(d, i, j, k) + cov8(d, i, j + 1, k)) / 2.f;
-    const float covz1 = (dzn[k + 1] * cov9(d, i, j, k) + dzn[k] * cov9(d, i, j, k + 1)) / (dzn[k] + dzn[k + 1]);
-    const float covc = covx1 + covy1 + covz1;
-    const float dfw1 = (-diu7(d, i, j, k) + diu7(d, i + 1, j, k)) / dx1[i] +
-                       (-diu8(d, i, j, k) + diu8(d, i, j + 1, k)) / dy1[j] +
-                       (-diu9(d, i, j, k) + diu9(d, i, j, k + 1)) / dzs[k];
-    const float df = d.vn * dfw1;
-    d.h[c] = (-covc + df);
-  }
-}
-
 // ------------------------------------------------------------------ feedbf.f95:35-61
 __global__ void __launch_bounds__(BX *BY) k_feedbf(LesDom d) {
   INTERIOR_IJK
@@ -187,23 +176,6 @@ __global__ void __launch_bounds__(BX *BY) k_feedbf(LesDom d) {
   d.h[c] = d.h[c] + fz;
 }
 
-// ------------------------------------------------------------------ les.f95:45-65
-__global__ void __launch_bounds__(BX *BY) k_les_sm(LesDom d) {
-  INTERIOR_IJK
-  const float dudxx1 = diu1(d, i, j, k);
-  const float dudyx1 = (diu2(d, i - 1, j, k) + diu2(d, i - 1, j + 1, k) + diu2(d, i, j, k) + diu2(d, i, j + 1, k)) * .25f;
-  const float dudzx1 = (diu3(d, i - 1, j, k) + diu3(d, i - 1, j, k + 1) + diu3(d, i, j, k) + diu3(d, i, j, k + 1)) * .25f;
-  const float dvdxx1 = (diu4(d, i, j, k) + diu4(d, i, j - 1, k) + diu4(d, i + 1, j, k) + diu4(d, i + 1, j - 1, k)) * .25f;
-  const float dvdyx1 = diu5(d, i, j, k);
-  const float dvdzx1 = (diu6(d, i, j - 1, k) + diu6(d, i, j - 1, k + 1) + diu6(d, i, j, k) + diu6(d, i, j, k + 1)) * .25f;
-  const float dwdxx1 = (diu7(d, i, j, k) + diu7(d, i, j, k - 1) + diu7(d, i + 1, j, k) + diu7(d, i + 1, j, k - 1)) * .25f;
-  const float dwdyx1 = (diu8(d, i, j, k) + diu8(d, i, j, k - 1) + diu8(d, i, j + 1, k) + diu8(d, i, j + 1, k - 1)) * .25f;
-  const float dwdzx1 = diu9(d, i, j, k);
-  const float cd = 0.1f * d.gr.delx1[k];
-  const float s1 = dudyx1 + dvdxx1, s2 = dwdyx1 + dvdzx1, s3 = dudzx1 + dwdxx1;
-  d.sm[lix(d, i, j, k)] =
-      cd * cd * __fsqrt_rn(2.f * (dudxx1 * dudxx1 + dvdyx1 * dvdyx1 + dwdzx1 * dwdzx1) + s1 * s1 + s2 * s2 + s3 * s3);
-}
 // boundsm.f95:18-64, three ordered phases
 __global__ void k_boundsm_i(LesDom d) {  // j = -1..jm+1, k = 0..km+1
   const int j = blockIdx.x * blockDim.x + threadIdx.x - 1;
@@ -225,120 +197,6 @@ __global__ void k_boundsm_k(LesDom d) {  // i = 0..im+1, j = -1..jm+1
   if (i > d.im + 1) return;
   d.sm[lix(d, i, j, 0)] = -d.sm[lix(d, i, j, 1)];
   d.sm[lix(d, i, j, d.km + 1)] = d.sm[lix(d, i, j, d.km)];
-}
-
-#define SM_(i, j, k) d.sm[lix(d, (i), (j), (k))]
-
-// viscous terms of f, g, h (les.f95:83-242), with the k = 1 wall functions
-__global__ void __launch_bounds__(BX *BY) k_les_visc(LesDom d) {
-  INTERIOR_IJK
-  const float *dx1 = d.gr.dx1, *dy1 = d.gr.dy1, *dzn = d.gr.dzn, *dxs = d.gr.dxs, *dys = d.gr.dys;
-  const int c = lix(d, i, j, k);
-  const float dxa = dx1[i] + dx1[i + 1];
-  const float dxb = dx1[i - 1] + dx1[i];
-  const float dya = dy1[j] + dy1[j + 1];
-  // x component
-  {
-    const float evsx2 = SM_(i + 1, j, k);
-    const float evsx1 = SM_(i, j, k);
-    const float evsy2 = (dy1[j + 1] * ((dx1[i + 1] * SM_(i, j, k) + dx1[i] * SM_(i + 1, j, k)) / dxa) +
-                         dy1[j] * ((dx1[i + 1] * SM_(i, j + 1, k) + dx1[i] * SM_(i + 1, j + 1, k)) / dxa)) / dya;
-    const float evsy1 = (dy1[j + 1] * ((dx1[i + 1] * SM_(i, j - 1, k) + dx1[i] * SM_(i + 1, j - 1, k)) / dxa) +
-                         dy1[j] * ((dx1[i + 1] * SM_(i, j, k) + dx1[i] * SM_(i + 1, j, k)) / dxa)) / dya;
-    float vfu;
-    if (k >= 2) {
-      const float evsz2 = (dzn[k + 1] * ((dx1[i + 1] * SM_(i, j, k) + dx1[i] * SM_(i + 1, j, k)) / dxa) +
-                           dzn[k] * ((dx1[i + 1] * SM_(i, j, k + 1) + dx1[i] * SM_(i + 1, j, k + 1)) / dxa)) /
-                          (dzn[k] + dzn[k + 1]);
-      const float evsz1 = (dzn[k] * ((dx1[i + 1] * SM_(i, j, k - 1) + dx1[i] * SM_(i + 1, j, k - 1)) / dxa) +
-                           dzn[k - 1] * ((dx1[i + 1] * SM_(i, j, k) + dx1[i] * SM_(i + 1, j, k)) / dxa)) /
-                          (dzn[k - 1] + dzn[k]);
-      const float visux2 = (evsx2) * 2.f * diu1(d, i + 1, j, k);
-      const float visux1 = (evsx1) * 2.f * diu1(d, i, j, k);
-      const float visuy2 = (evsy2) * (diu2(d, i, j + 1, k) + diu4(d, i + 1, j, k));
-      const float visuy1 = (evsy1) * (diu2(d, i, j, k) + diu4(d, i + 1, j - 1, k));
-      const float visuz2 = (evsz2) * (diu3(d, i, j, k + 1) + diu7(d, i + 1, j, k));
-      const float visuz1 = (evsz1) * (diu3(d, i, j, k) + diu7(d, i + 1, j, k - 1));
-      vfu = (visux2 - visux1) / dxs[i] + (visuy2 - visuy1) / dy1[j] + (visuz2 - visuz1) / dzn[k];
-    } else {  // wall function (les.f95:118-139): y and z terms appear twice, as written
-      const float evsz2 = (dzn[2] * ((dx1[i + 1] * SM_(i, j, 1) + dx1[i] * SM_(i + 1, j, 1)) / dxa) +
-                           dzn[1] * ((dx1[i + 1] * SM_(i, j, 2) + dx1[i] * SM_(i + 1, j, 2)) / dxa)) /
-                          (dzn[1] + dzn[2]);
-      const float visux2 = (evsx2) * 2.f * diu1(d, i + 1, j, 1);
-      const float visux1 = (evsx1) * 2.f * diu1(d, i, j, 1);
-      const float visuy2 = (evsy2) * (diu2(d, i, j + 1, 1) + diu4(d, i + 1, j, 1));
-      const float visuy1 = (evsy1) * (diu2(d, i, j, 1) + diu4(d, i + 1, j - 1, 1));
-      const float visuz2 = (evsz2) * (diu3(d, i, j, 2) + diu7(d, i + 1, j, 1));
-      const float r = U_(i, j, 1) / uspd_raw(d, i, j);  // uspd after vel2.f95:353
-      const float t = 0.4f * r / d.logz;
-      const float visuz1 = t * t * r;
-      vfu = (visux2 - visux1) / dxs[i] + (visuy2 - visuy1) / dy1[j] + (visuz2 - visuz1) / dzn[1] +
-            (visuy2 - visuy1) / dy1[j] + (visuz2 - visuz1) / dzn[1];
-    }
-    d.f[c] = (d.f[c] + vfu);
-  }
-  // y component
-  {
-    const float evsy2 = SM_(i, j + 1, k);
-    const float evsy1 = SM_(i, j, k);
-    const float evsx2 = (dy1[j + 1] * ((dx1[i + 1] * SM_(i, j, k) + dx1[i] * SM_(i + 1, j, k)) / dxa) +
-                         dy1[j] * ((dx1[i + 1] * SM_(i, j + 1, k) + dx1[i] * SM_(i + 1, j + 1, k)) / dxa)) / dya;
-    const float evsx1 = (dy1[j + 1] * ((dx1[i] * SM_(i - 1, j, k) + dx1[i - 1] * SM_(i, j, k)) / dxb) +
-                         dy1[j] * ((dx1[i] * SM_(i - 1, j + 1, k) + dx1[i - 1] * SM_(i, j + 1, k)) / dxb)) / dya;
-    float vfv;
-    if (k >= 2) {
-      const float evsz2 = (dzn[k + 1] * ((dx1[i + 1] * SM_(i, j, k) + dx1[i] * SM_(i + 1, j, k)) / dxa) +
-                           dzn[k] * ((dx1[i + 1] * SM_(i, j, k + 1) + dx1[i] * SM_(i + 1, j, k + 1)) / dxa)) /
-                          (dzn[k] + dzn[k + 1]);
-      const float evsz1 = (dzn[k] * ((dx1[i + 1] * SM_(i, j, k - 1) + dx1[i] * SM_(i + 1, j, k - 1)) / dxa) +
-                           dzn[k - 1] * ((dx1[i + 1] * SM_(i, j, k) + dx1[i] * SM_(i + 1, j, k)) / dxa)) /
-                          (dzn[k - 1] + dzn[k]);
-      const float visvx2 = (evsx2) * (diu2(d, i, j + 1, k) + diu4(d, i + 1, j, k));
-      const float visvx1 = (evsx1) * (diu2(d, i - 1, j + 1, k) + diu4(d, i, j, k));
-      const float visvy2 = (evsy2) * 2.f * diu5(d, i, j + 1, k);
-      const float visvy1 = (evsy1) * 2.f * diu5(d, i, j, k);
-      const float visvz2 = (evsz2) * (diu6(d, i, j, k + 1) + diu8(d, i, j + 1, k));
-      const float visvz1 = (evsz1) * (diu6(d, i, j, k) + diu8(d, i, j + 1, k - 1));
-      vfv = (visvx2 - visvx1) / dx1[i] + (visvy2 - visvy1) / dys[j] + (visvz2 - visvz1) / dzn[k];
-    } else {  // wall function (les.f95:178-201)
-      const float evsz2 = (dzn[2] * ((dx1[i + 1] * SM_(i, j, 1) + dx1[i] * SM_(i + 1, j, 1)) / dxa) +
-                           dzn[1] * ((dx1[i + 1] * SM_(i, j, 2) + dx1[i] * SM_(i + 1, j, 2)) / dxa)) /
-                          (dzn[1] + dzn[2]);
-      const float visvx2 = (evsx2) * (diu2(d, i, j + 1, 1) + diu4(d, i + 1, j, 1));
-      const float visvx1 = (evsx1) * (diu2(d, i - 1, j + 1, 1) + diu4(d, i, j, 1));
-      const float visvy2 = (evsy2) * 2.f * diu5(d, i, j + 1, 1);
-      const float visvy1 = (evsy1) * 2.f * diu5(d, i, j, 1);
-      const float visvz2 = (evsz2) * (diu6(d, i, j, 2) + diu8(d, i, j + 1, 1));
-      const float r = V_(i, j, 1) / vspd_raw(d, i, j);  // vspd after vel2.f95:354
-      const float t = 0.4f * r / d.logz;
-      const float visvz1 = t * t * r;
-      vfv = (visvx2 - visvx1) / dx1[i] + (visvy2 - visvy1) / dys[j] + (visvz2 - visvz1) / dzn[1];
-    }
-    d.g[c] = (d.g[c] + vfv);
-  }
-  // z component, k = 1..km
-  {
-    const float dzc = dzn[k] + dzn[k + 1];
-    const float evsz2 = SM_(i, j, k + 1);
-    const float evsz1 = SM_(i, j, k);
-    const float evsx2 = (dzn[k + 1] * ((dx1[i + 1] * SM_(i, j, k) + dx1[i] * SM_(i + 1, j, k)) / dxa) +
-                         dzn[k] * ((dx1[i + 1] * SM_(i, j, k + 1) + dx1[i] * SM_(i + 1, j, k + 1)) / dxa)) / dzc;
-    const float evsx1 = (dzn[k + 1] * ((dx1[i] * SM_(i - 1, j, k) + dx1[i - 1] * SM_(i, j, k)) / dxb) +
-                         dzn[k] * ((dx1[i] * SM_(i - 1, j, k + 1) + dx1[i - 1] * SM_(i, j, k + 1)) / dxb)) / dzc;
-    const float evsy2 = (dzn[k + 1] * ((dy1[j + 1] * SM_(i, j, k) + dy1[j] * SM_(i, j + 1, k)) / dya) +
-                         dzn[k] * ((dy1[j + 1] * SM_(i, j, k + 1) + dy1[j] * SM_(i, j + 1, k + 1)) / dya)) / dzc;
-    const float dyb = dy1[j - 1] + dy1[j];
-    const float evsy1 = (dzn[k + 1] * ((dy1[j] * SM_(i, j - 1, k) + dy1[j - 1] * SM_(i, j, k)) / dyb) +
-                         dzn[k] * ((dy1[j] * SM_(i, j - 1, k + 1) + dy1[j - 1] * SM_(i, j, k + 1)) / dyb)) / dzc;
-    const float viswx2 = (evsx2) * (diu3(d, i, j, k + 1) + diu7(d, i + 1, j, k));
-    const float viswx1 = (evsx1) * (diu3(d, i - 1, j, k + 1) + diu7(d, i, j, k));
-    const float viswy2 = (evsy2) * (diu6(d, i, j, k + 1) + diu8(d, i, j + 1, k));
-    const float viswy1 = (evsy1) * (diu6(d, i, j - 1, k + 1) + diu8(d, i, j, k));
-    const float viswz2 = (evsz2) * 2.f * diu9(d, i, j, k + 1);
-    const float viswz1 = (evsz1) * 2.f * diu9(d, i, j, k);
-    const float vfw = (viswx2 - viswx1) / dx1[i] + (viswy2 - viswy1) / dy1[j] + (viswz2 - viswz1) / dzn[k];
-    d.h[c] = (d.h[c] + vfw);
-  }
 }
 
 // ------------------------------------------------------------------ adam.f95:30-44
@@ -370,22 +228,49 @@ __global__ void k_bondfg(LesDom d) {
 }
 
 // ------------------------------------------------------------------ press.f95:49-60
-// rhs, plus the FP64 block partials of sum(dx1*dy1*dzn*rhs) (press.f95:63-72)
-// dst: the rhs array (rhs = d.rhs) or the SOR's internal rhs buffer, which also takes
-// periodic ghost copies of rows 1, 2, jm-1, jm in rows jm+1, jm+2, -1, 0.
-__global__ void __launch_bounds__(BX *BY) k_rhs(LesDom d, float *dst, int ghost) {
-  __shared__ double sh[32];
-  const int i = blockIdx.x * BX + threadIdx.x + 1;
-  const int j = blockIdx.y * BY + threadIdx.y + 1;
-  const int k = blockIdx.z + 1;
-  double term = 0.0;
-  if (i <= d.im && j <= d.jm) {
-    const float *dx1 = d.gr.dx1, *dy1 = d.gr.dy1, *dzn = d.gr.dzn;
-    const int c = lix(d, i, j, k);
-    const float r = (-d.u[c - 1] + d.u[c]) / dx1[i] + (-d.v[c - d.pi] + d.v[c]) / dy1[j] +
-                    (-d.w[c - d.np] + d.w[c]) / dzn[k];
-    const float rr = (d.f[c] - d.f[c - 1]) / dx1[i] + (d.g[c] - d.g[c - d.pi]) / dy1[j] +
-                     (d.h[c] - d.h[c - d.np]) / dzn[k] + r / d.dt;
+// (u, v, w, f, g, h are only read here: read-only loads)
+template <bool P2, bool ZF>
+__device__ __forceinline__ float rhs_cell(const LesDom &d, int i, int j, int k, int c, unsigned &bd) {
+  const float *dx1 = d.gr.dx1, *dy1 = d.gr.dy1, *dzn = d.gr.dzn;
+  const float rx = d.gr.rdx1[i], ry = d.gr.rdy1[j], rz = d.gr.rdzn[k];
+  const float *u = d.u, *v = d.v, *w = d.w, *f = d.f, *g = d.g, *h = d.h;
+  const float r = dvs<P2, ZF>(-__ldg(u + c - 1) + __ldg(u + c), dx1[i], rx, bd) +
+                  dvs<P2, ZF>(-__ldg(v + c - d.pi) + __ldg(v + c), dy1[j], ry, bd) +
+                  dvz<ZF>(-__ldg(w + c - d.np) + __ldg(w + c), dzn[k], rz, bd);
+  return dvs<P2, ZF>(__ldg(f + c) - __ldg(f + c - 1), dx1[i], rx, bd) +
+         dvs<P2, ZF>(__ldg(g + c) - __ldg(g + c - d.pi), dy1[j], ry, bd) +
+         dvz<ZF>(__ldg(h + c) - __ldg(h + c - d.np), dzn[k], rz, bd) + dvz<ZF>(r, d.dt, d.rdt, bd);
+}
+// Block sum of one FP32 term per thread (BX x BY threads) into part[slot]: warp pairs
+// (warp_sum_pair), then the warps in FP64 in order.
+__device__ __forceinline__ void block_part(const LesDom &d, float term, int slot) {
+  __shared__ double sh[BX * BY / 32];
+  const int tid = threadIdx.y * BX + threadIdx.x;
+  const double x = warp_sum_pair(term);
+  if ((tid & 31) == 0) sh[tid >> 5] = x;
+  __syncthreads();
+  if (tid == 0) {
+    double s = 0.0;
+    for (int q = 0; q < BX * BY / 32; ++q) s += sh[q];
+    d.part[slot] = s;
+  }
+}
+
+// rhs of the block (bx, by, bz) of grid g, plus its partial of
+// sum(dx1*dy1*dzn*rhs) (press.f95:63-72).  dst: the rhs array (rhs = d.rhs) or the
+// SOR's internal rhs buffer, which also takes periodic ghost copies of rows 1, 2,
+// jm-1, jm in rows jm+1, jm+2, -1, 0.  ZF as in velnw_block.
+template <bool P2, bool ZF>
+__device__ __forceinline__ void rhs_block(const LesDom &d, float *dst, int ghost, int bx, int by, int bz, uint3 g) {
+  const int i0 = bx * BX + threadIdx.x + 1, j0 = by * BY + threadIdx.y + 1, k = bz + 1;
+  const bool in = (i0 <= d.im && j0 <= d.jm);
+  const int i = min(i0, d.im), j = min(j0, d.jm);  // past the edge: the edge cell again, not stored
+  const int c = lix(d, i, j, k);
+  unsigned bd = 0;
+  const float rr = rhs_cell<P2, ZF>(d, i, j, k, c, bd);
+  if (ZF && defer_block(bd, d.fix[FIX_RHS])) return;
+  float term = 0.f;
+  if (in) {
     dst[c] = rr;
     if (ghost) {
       if (j == 1) dst[lix(d, i, d.jm + 1, k)] = rr;
@@ -393,54 +278,58 @@ __global__ void __launch_bounds__(BX *BY) k_rhs(LesDom d, float *dst, int ghost)
       if (j == d.jm - 1) dst[lix(d, i, -1, k)] = rr;
       if (j == d.jm) dst[lix(d, i, 0, k)] = rr;
     }
-    term = (double)(dx1[i] * dy1[j] * dzn[k] * rr);
+    term = d.gr.dx1[i] * d.gr.dy1[j] * d.gr.dzn[k] * rr;
   }
-  const int tid = threadIdx.y * BX + threadIdx.x;
-  double x = term;
-  for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-  if ((tid & 31) == 0) sh[tid >> 5] = x;
-  __syncthreads();
-  if (tid == 0) {
-    double s = 0.0;
-    for (int q = 0; q < BX * BY / 32; ++q) s += sh[q];
-    d.part[(blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = s;
-  }
+  block_part(d, term, (int)((bz * g.y + by) * g.x + bx));
+}
+template <bool P2, bool ZF>
+__global__ void __launch_bounds__(BX *BY) k_rhs(LesDom d, float *dst, int ghost) {
+  rhs_block<P2, ZF>(d, dst, ghost, blockIdx.x, blockIdx.y, blockIdx.z, make_uint3(gridDim.x, gridDim.y, gridDim.z));
+}
+template <bool P2>
+__global__ void __launch_bounds__(BX *BY) k_rhs_fix(LesDom d, float *dst, int ghost, uint3 g) {
+  for_deferred(d.fix[FIX_RHS], g, [&](int bx, int by, int bz) { rhs_block<P2, false>(d, dst, ghost, bx, by, bz, g); });
 }
 // pav partials: sum(p*dx1*dy1*dzn) (press.f95:124-133)
 __global__ void __launch_bounds__(BX *BY) k_pav_part(LesDom d) {
-  __shared__ double sh[32];
   const int i = blockIdx.x * BX + threadIdx.x + 1;
   const int j = blockIdx.y * BY + threadIdx.y + 1;
   const int k = blockIdx.z + 1;
-  double term = 0.0;
-  if (i <= d.im && j <= d.jm) {
-    term = (double)(d.p[lix(d, i, j, k)] * d.gr.dx1[i] * d.gr.dy1[j] * d.gr.dzn[k]);
-  }
-  const int tid = threadIdx.y * BX + threadIdx.x;
-  double x = term;
-  for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-  if ((tid & 31) == 0) sh[tid >> 5] = x;
-  __syncthreads();
-  if (tid == 0) {
-    double s = 0.0;
-    for (int q = 0; q < BX * BY / 32; ++q) s += sh[q];
-    d.part[(blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = s;
-  }
+  float term = 0.f;
+  if (i <= d.im && j <= d.jm) term = __ldg(d.p + lix(d, i, j, k)) * d.gr.dx1[i] * d.gr.dy1[j] * d.gr.dzn[k];
+  block_part(d, term, (int)((blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x));
 }
-// mean = (float)(sum of partials / area); one block, fixed order
-__global__ void __launch_bounds__(1024) k_finish_mean(LesDom d, int nparts, int slot) {
-  __shared__ double sh[32];
+// mean = (float)(sum of partials / area), summed in a fixed order: FIN_BLOCKS chunks,
+// each a strided FP64 sum and a fixed tree, then the chunks in order by the last block
+constexpr int FIN_BLOCKS = 128, FIN_THREADS = 256;
+__global__ void __launch_bounds__(FIN_THREADS) k_finish_mean(LesDom d, int nparts, int slot) {
+  __shared__ double sh[FIN_THREADS / 32];
+  __shared__ int last;
+  const int chunk = (nparts + FIN_BLOCKS - 1) / FIN_BLOCKS;
+  const int lo = blockIdx.x * chunk, hi = min(nparts, lo + chunk);
   double s = 0.0;
-  for (int q = threadIdx.x; q < nparts; q += blockDim.x) s += d.part[q];
+  for (int q = lo + (int)threadIdx.x; q < hi; q += FIN_THREADS) s += d.part[q];
   for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
   if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
   __syncthreads();
   if (threadIdx.x == 0) {
     double t = 0.0;
-    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += sh[q];
+    for (int q = 0; q < FIN_THREADS / 32; ++q) t += sh[q];
+    d.part2[blockIdx.x] = t;
+    __threadfence();
+    last = (atomicAdd(d.cnt + 8, 1u) == FIN_BLOCKS - 1);
+  }
+  __syncthreads();
+  if (!last || threadIdx.x >= 32) return;
+  __threadfence();
+  double t = 0.0;
+  for (int q = (int)threadIdx.x; q < FIN_BLOCKS; q += 32) t += __ldcg(d.part2 + q);
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+  if (threadIdx.x == 0) {
     const float mean = (float)(t / d.scal[SC_AREA]);
     d.fscal[slot] = mean;
     d.scal[slot] = (double)mean;
+    d.cnt[8] = 0u;
   }
 }
 __global__ void __launch_bounds__(BX *BY) k_sub_mean(LesDom d, float *a, int slot) {
@@ -554,8 +443,39 @@ __global__ void __launch_bounds__(BX *BY) k_count_nonfinite(LesDom d, unsigned l
     ++*(ctx).nlaunch;                   \
   } while (0)
 
+// the kernel variant for the domain's spacing modes (power-of-two x/y, div_k range)
+#define LES_PZ_SWITCH(d, K, ...)                            \
+  do {                                                      \
+    if ((d).xy_pow2 && (d).zfast) K<true, true>__VA_ARGS__; \
+    else if ((d).xy_pow2) K<true, false>__VA_ARGS__;        \
+    else if ((d).zfast) K<false, true>__VA_ARGS__;          \
+    else K<false, false>__VA_ARGS__;                        \
+  } while (0)
+
+// the fixup grid of a deferred-block list: a few CTAs per SM at most
+inline unsigned fix_grid(const LesDom &d, dim3 g) {
+  return std::min<unsigned>(g.x * g.y * g.z, (unsigned)std::max(1, 2 * d.sms));
+}
+inline uint3 u3(dim3 g) { return make_uint3(g.x, g.y, g.z); }
+
 void les_launch_velnw(const LesDom &d, LesCtx ctx) {
-  LAUNCH(ctx, k_velnw<<<interior_grid(d, d.km), dim3(BX, BY), 0, ctx.s>>>(d));
+  const dim3 g = interior_grid(d, d.km), b(BX, BY);
+  LAUNCH(ctx, LES_PZ_SWITCH(d, k_velnw, <<<g, b, 0, ctx.s>>>(d)));
+  if (d.zfast) {
+    if (d.xy_pow2) LAUNCH(ctx, (k_velnw_fix<true><<<fix_grid(d, g), b, 0, ctx.s>>>(d, u3(g))));
+    else LAUNCH(ctx, (k_velnw_fix<false><<<fix_grid(d, g), b, 0, ctx.s>>>(d, u3(g))));
+  }
+}
+
+// rhs into dst, its fixup, and the mean
+static void launch_rhs(const LesDom &d, float *dst, int ghost, LesCtx ctx) {
+  const dim3 g = interior_grid(d, d.km), b(BX, BY);
+  LAUNCH(ctx, LES_PZ_SWITCH(d, k_rhs, <<<g, b, 0, ctx.s>>>(d, dst, ghost)));
+  if (d.zfast) {
+    if (d.xy_pow2) LAUNCH(ctx, (k_rhs_fix<true><<<fix_grid(d, g), b, 0, ctx.s>>>(d, dst, ghost, u3(g))));
+    else LAUNCH(ctx, (k_rhs_fix<false><<<fix_grid(d, g), b, 0, ctx.s>>>(d, dst, ghost, u3(g))));
+  }
+  LAUNCH(ctx, k_finish_mean<<<FIN_BLOCKS, FIN_THREADS, 0, ctx.s>>>(d, (int)(g.x * g.y * g.z), SC_RHSAV));
 }
 
 void les_launch_bondv1(const LesDom &d, int n, LesCtx ctx) {
@@ -569,20 +489,15 @@ void les_launch_bondv1(const LesDom &d, int n, LesCtx ctx) {
   LAUNCH(ctx, k_bondv1_topbottom<<<dim3((d.im + 2 + 127) / 128, d.jm + 3), 128, 0, ctx.s>>>(d));
 }
 
-void les_launch_velfg(const LesDom &d, LesCtx ctx) {
-  LAUNCH(ctx, k_velfg<<<interior_grid(d, d.km), dim3(BX, BY), 0, ctx.s>>>(d));
-}
 
 void les_launch_feedbf(const LesDom &d, LesCtx ctx) {
   LAUNCH(ctx, k_feedbf<<<interior_grid(d, d.km), dim3(BX, BY), 0, ctx.s>>>(d));
 }
 
-void les_launch_les(const LesDom &d, LesCtx ctx) {
-  LAUNCH(ctx, k_les_sm<<<interior_grid(d, d.km), dim3(BX, BY), 0, ctx.s>>>(d));
+void les_launch_boundsm(const LesDom &d, LesCtx ctx) {
   LAUNCH(ctx, k_boundsm_i<<<dim3((d.jm + 3 + 127) / 128, d.km + 2), 128, 0, ctx.s>>>(d));
   LAUNCH(ctx, k_boundsm_j<<<dim3((d.im + 2 + 127) / 128, d.km + 2), 128, 0, ctx.s>>>(d));
   LAUNCH(ctx, k_boundsm_k<<<dim3((d.im + 2 + 127) / 128, d.jm + 3), 128, 0, ctx.s>>>(d));
-  LAUNCH(ctx, k_les_visc<<<interior_grid(d, d.km), dim3(BX, BY), 0, ctx.s>>>(d));
 }
 
 void les_launch_adam(const LesDom &d, LesCtx ctx) {
@@ -609,17 +524,11 @@ int les_interior_blocks(const LesDom &d) {
 }
 
 void les_launch_rhs_mean(const LesDom &d, LesCtx ctx) {
-  const int nb = les_interior_blocks(d);
-  LAUNCH(ctx, k_rhs<<<interior_grid(d, d.km), dim3(BX, BY), 0, ctx.s>>>(d, d.rhs, 0));
-  LAUNCH(ctx, k_finish_mean<<<1, 1024, 0, ctx.s>>>(d, nb, SC_RHSAV));
+  launch_rhs(d, d.rhs, 0, ctx);
   LAUNCH(ctx, k_sub_mean<<<interior_grid(d, d.km), dim3(BX, BY), 0, ctx.s>>>(d, d.rhs, SC_RHSAV));
 }
 
-void les_launch_rhs_sor(const LesDom &d, LesCtx ctx) {
-  const int nb = les_interior_blocks(d);
-  LAUNCH(ctx, k_rhs<<<interior_grid(d, d.km), dim3(BX, BY), 0, ctx.s>>>(d, d.sorR, 1));
-  LAUNCH(ctx, k_finish_mean<<<1, 1024, 0, ctx.s>>>(d, nb, SC_RHSAV));
-}
+void les_launch_rhs_sor(const LesDom &d, LesCtx ctx) { launch_rhs(d, d.sorR, 1, ctx); }
 
 void les_launch_sor_begin(const LesDom &d, LesCtx ctx) {
   LAUNCH(ctx, k_sor_begin<<<1, 1, 0, ctx.s>>>(d));
@@ -647,7 +556,7 @@ int les_sor_simple_parts(const LesDom &d) {
 void les_launch_pav_adjust(const LesDom &d, LesCtx ctx) {
   const int nb = les_interior_blocks(d);
   LAUNCH(ctx, k_pav_part<<<interior_grid(d, d.km), dim3(BX, BY), 0, ctx.s>>>(d));
-  LAUNCH(ctx, k_finish_mean<<<1, 1024, 0, ctx.s>>>(d, nb, SC_PAV));
+  LAUNCH(ctx, k_finish_mean<<<FIN_BLOCKS, FIN_THREADS, 0, ctx.s>>>(d, nb, SC_PAV));
   LAUNCH(ctx, k_sub_mean<<<interior_grid(d, d.km), dim3(BX, BY), 0, ctx.s>>>(d, d.p, SC_PAV));
   les_launch_boundp1(d, ctx, 0);
   les_launch_boundp2(d, ctx, 0);

@@ -13,9 +13,11 @@ struct LesCtx {
 // per-subroutine kernels (les_kernels.cu)
 void les_launch_velnw(const LesDom &d, LesCtx ctx);
 void les_launch_bondv1(const LesDom &d, int n, LesCtx ctx);
-void les_launch_velfg(const LesDom &d, LesCtx ctx);
 void les_launch_feedbf(const LesDom &d, LesCtx ctx);
-void les_launch_les(const LesDom &d, LesCtx ctx);
+void les_launch_boundsm(const LesDom &d, LesCtx ctx);
+// les_fused.cu: velfg (optionally with feedbf) and les (optionally with adam)
+void les_launch_velfg_fused(const LesDom &d, bool with_feedbf, LesCtx ctx);
+void les_launch_les_fused(const LesDom &d, bool with_adam, LesCtx ctx);
 void les_launch_adam(const LesDom &d, LesCtx ctx);
 void les_launch_bondfg(const LesDom &d, LesCtx ctx);
 void les_launch_boundp1(const LesDom &d, LesCtx ctx, int obey_converged);

@@ -73,10 +73,8 @@ static void enqueue_sor_fused(const LesDom &d, const les_params &prm, int ny, co
 void les_step_enqueue(const LesDom &d, const les_params &prm, int ny, const LesSorMaps *maps, int n, LesCtx ctx) {
   les_launch_velnw(d, ctx);
   les_launch_bondv1(d, n, ctx);
-  les_launch_velfg(d, ctx);
-  les_launch_feedbf(d, ctx);
-  les_launch_les(d, ctx);
-  les_launch_adam(d, ctx);
+  les_launch_velfg_fused(d, true, ctx);  // velfg + feedbf
+  les_launch_les_fused(d, true, ctx);    // les + adam
   les_launch_bondfg(d, ctx);
   if (ny > 0) {
     les_launch_rhs_sor(d, ctx);
@@ -134,11 +132,5 @@ int les_step_sor_pass(const LesDom &d, const les_params &prm, LesStepPlan *plan,
   enqueue_sor_fused(d, ten, ny, &plan->maps, ctx);
   return 10;
 }
-void les_step_velfg_pass(const LesDom &d, LesCtx ctx) {
-  les_launch_velfg(d, ctx);
-  les_launch_feedbf(d, ctx);
-}
-void les_step_les_pass(const LesDom &d, LesCtx ctx) {
-  les_launch_les(d, ctx);
-  les_launch_adam(d, ctx);
-}
+void les_step_velfg_pass(const LesDom &d, LesCtx ctx) { les_launch_velfg_fused(d, true, ctx); }
+void les_step_les_pass(const LesDom &d, LesCtx ctx) { les_launch_les_fused(d, true, ctx); }

@@ -35,7 +35,8 @@ def _run_pair(sc, nsteps, params, prec, **rkw):
 
 
 @pytest.mark.parametrize("shape,nmaxp", [((48, 32, 16), 20), ((130, 46, 12), 7), ((37, 6, 9), 9),
-                                         ((61, 21, 10), 6), ((250, 100, 20), 50), ((121, 2, 5), 3)])
+                                         ((61, 21, 10), 6), ((250, 100, 20), 50), ((121, 2, 5), 3),
+                                         ((50, 30, 12), 1)])
 def test_step_matches_stage_sequence(built_lib, shape, nmaxp):
     """The fused/graph step equals the per-subroutine entry points bit for bit.
 
@@ -75,9 +76,28 @@ def test_step_after_uploading_state(built_lib):
             assert np.array_equal(x.view(np.uint32), y.view(np.uint32)), (n, lesgpu.FIELD_NAMES[fid])
 
 
-@pytest.mark.parametrize("shape,nsteps", [((48, 32, 24), 10), ((40, 64, 20), 6)])
-def test_steps_vs_fp32_oracle(built_lib, shape, nsteps):
-    sc = scenario(*shape, seed=21)
+@pytest.mark.parametrize("spacing", [(4.0, 4.0), (3.0, 5.0)])
+def test_step_reciprocal_division_matches_ieee(built_lib, monkeypatch, spacing):
+    """The reciprocal-corrected divisions (and the power-of-two multiplications) give
+    the same step as IEEE divisions everywhere, bit for bit."""
+    sc = scenario(48, 30, 14, seed=61, dx=spacing[0], dy=spacing[1])
+    params = lesgpu.Params(nmaxp=8)
+    a = make_gpu(sc, params)
+    monkeypatch.setenv("LES_IEEE_DIV", "1")
+    b = make_gpu(sc, params)
+    monkeypatch.delenv("LES_IEEE_DIV")
+    for n in range(1, 6):
+        a.step(n, 5)
+        b.step(n, 5)
+    for fid in lesgpu.STATE_FIELDS:
+        x, y = a.download(fid), b.download(fid)
+        assert np.array_equal(x.view(np.uint32), y.view(np.uint32)), lesgpu.FIELD_NAMES[fid]
+
+
+@pytest.mark.parametrize("shape,nsteps,spacing", [((48, 32, 24), 10, (4.0, 4.0)), ((40, 64, 20), 6, (4.0, 4.0)),
+                                                  ((44, 30, 16), 6, (3.0, 5.0))])
+def test_steps_vs_fp32_oracle(built_lib, shape, nsteps, spacing):
+    sc = scenario(*shape, seed=21, dx=spacing[0], dy=spacing[1])
     params = lesgpu.Params()
     gpu, orc = _run_pair(sc, nsteps, params, 4, sqrt_half=1, red64=1)
     for fid, nm in FIELDS:
