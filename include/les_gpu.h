@@ -182,6 +182,19 @@ int les_gpu_diag(les_handle *h, double out[5]);
 int les_gpu_check_finite(les_handle *h, long long *bad);
 /* The handle's CUDA stream (a cudaStream_t), for callers that time or overlap work. */
 int les_gpu_stream(les_handle *h, void **stream);
+/* Volume-weighted interior mean of a 3-D field, sum(x*dx1*dy1*dzn)/sum(dx1*dy1*dzn)
+ * over i=1..im, j=1..jm, k=1..km, in the order and FP32 rounding press uses for pav
+ * (press.f95:124-133); the field is not changed.  No counterpart in the reference:
+ * an addition for callers that must not allocate device memory when they call (a
+ * pre-sized memory cap, a host allocator that owns the device, a monitor between
+ * steps).  It allocates nothing: its scratch is one static device array per device,
+ * shared by all calls, which keeps what the last call left (each call clears what must
+ * start at zero).  Calls that overlap in time race on it.  The array's address is
+ * looked up on the first call from a device: make that call outside stream capture.
+ * Domains with more than LES_NOALLOC_MAX_PARTS interior blocks ((im+63)/64 *
+ * (jm+3)/4 * km) are refused with LES_ERR_ARG.  Synchronises the handle's stream. */
+#define LES_NOALLOC_MAX_PARTS 262144 /* 2 MiB of FP64 block partials */
+int les_gpu_field_mean_noalloc(les_handle *h, int field, double *mean);
 /* Kernel launches issued on this handle since creation (all stages). */
 long long les_gpu_launch_count(les_handle *h);
 int les_gpu_last_error(les_handle *h, char *buf, size_t len);

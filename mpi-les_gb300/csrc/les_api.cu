@@ -583,6 +583,28 @@ extern "C" int les_gpu_setup_scenario(les_handle *h, const les_scenario *sc) {
     if (!(h)->committed) return fail((h), LES_ERR_STATE, "les_gpu_commit_setup not called"); \
   } while (0)
 
+// les_noalloc.cu
+int les_noalloc_interior_mean(const LesDom &dom, const float *x, const double *area_dev, cudaStream_t s,
+                              long long *nlaunch, int dev, double *mean, std::string *err);
+
+extern "C" int les_gpu_field_mean_noalloc(les_handle *h, int field, double *mean) {
+  if (!h || !mean) return LES_ERR_ARG;
+  if (field < LES_FIELD_U || field > LES_FIELD_SM)
+    return fail(h, LES_ERR_ARG, "field_mean_noalloc: field must be a 3-D field (LES_FIELD_U .. LES_FIELD_SM)");
+  LesDom shape{};
+  shape.im = h->dims.im; shape.jm = h->dims.jm; shape.km = h->dims.km;
+  const long long nparts = les_interior_blocks(shape);
+  if (nparts > LES_NOALLOC_MAX_PARTS)
+    return fail(h, LES_ERR_ARG, "field_mean_noalloc: the domain has " + std::to_string(nparts) +
+                                    " interior blocks ((im+63)/64*(jm+3)/4*km); the static scratch holds " +
+                                    std::to_string(LES_NOALLOC_MAX_PARTS));
+  NEED_COMMIT(h);
+  std::string err;
+  const int rc = les_noalloc_interior_mean(h->dom, h->fields[field - 1], h->scal_d + SC_AREA, h->s, &h->nlaunch,
+                                           h->dev, mean, &err);
+  return rc ? fail(h, rc, err) : LES_OK;
+}
+
 extern "C" int les_gpu_velnw(les_handle *h) {
   NEED_COMMIT(h);
   les_launch_velnw(h->dom, ctx_of(h));

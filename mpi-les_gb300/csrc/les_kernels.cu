@@ -301,7 +301,7 @@ __global__ void __launch_bounds__(BX *BY) k_pav_part(LesDom d) {
 }
 // mean = (float)(sum of partials / area), summed in a fixed order: FIN_BLOCKS chunks,
 // each a strided FP64 sum and a fixed tree, then the chunks in order by the last block
-constexpr int FIN_BLOCKS = 128, FIN_THREADS = 256;
+constexpr int FIN_BLOCKS = LES_FIN_BLOCKS, FIN_THREADS = 256;
 __global__ void __launch_bounds__(FIN_THREADS) k_finish_mean(LesDom d, int nparts, int slot) {
   __shared__ double sh[FIN_THREADS / 32];
   __shared__ int last;
@@ -551,6 +551,11 @@ void les_launch_sor_simple(const LesDom &d, int nmaxp, LesCtx ctx) {
 int les_sor_simple_parts(const LesDom &d) {
   const dim3 gs((d.im / 2 + 1 + BX - 1) / BX, (d.jm + BY - 1) / BY, d.km);
   return 2 * (int)(gs.x * gs.y * gs.z);
+}
+
+void les_launch_interior_mean(const LesDom &d, LesCtx ctx) {
+  LAUNCH(ctx, k_pav_part<<<interior_grid(d, d.km), dim3(BX, BY), 0, ctx.s>>>(d));
+  LAUNCH(ctx, k_finish_mean<<<FIN_BLOCKS, FIN_THREADS, 0, ctx.s>>>(d, les_interior_blocks(d), SC_PAV));
 }
 
 void les_launch_pav_adjust(const LesDom &d, LesCtx ctx) {
