@@ -7,6 +7,10 @@ noise, dt = 0.05 s, 50 red-black SOR iterations per step.  A "step" is one full 
 step of the reference's solver loop (velnw .. press).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--dims IMxJMxKM] [--no-cpu]
+
+--dims runs a smaller domain of the same kind (profiling captures: ncu wants a small
+case); --no-cpu skips the CPU baseline leg.  The headline line uses the defaults.
 
 One JSON line on stdout (rank 0).  Under torchrun each rank advances its own
 independent domain (replicas; the single domain does not shard without a halo
@@ -48,7 +52,7 @@ def workload_config(im=IM, jm=JM, km=KM):
             "im": im, "jm": jm, "km": km, "dx_m": 4.0, "dz0_m": 2.0, "dz_ratio": 1.04,
             "buildings": "seeded rectangular blocks, 30% plan coverage, 5-20 cells, 10-60 m",
             "inflow": "5 m/s*(z/100 m)^0.2 + uniform +-1e-3 m/s", "dt_s": 0.05, "sor_iters": SOR_ITERS,
-            "l2": "inputs larger than L2 (about 2.1 GB of fields per domain)"}
+            "l2": "inputs larger than L2 (about 3.8 GB of fields per domain)"}
 
 
 def scenario(seed=1, im=IM, jm=JM, km=KM):
@@ -212,9 +216,10 @@ def run_ours(args):
     if not os.path.exists(lesgpu.LIB_PATH):
         import __graft_entry__
         __graft_entry__.build()
+    IM, JM, KM = args.dims
     cells = IM * JM * KM
     dom = lesgpu.Domain(IM, JM, KM, lesgpu.Params())
-    dom.setup_scenario(scenario(seed=1 + rank))
+    dom.setup_scenario(scenario(seed=1 + rank, im=IM, jm=JM, km=KM))
     stream = torch.cuda.ExternalStream(dom.stream())
     nmax = args.warmup + args.steps + 10**6
     n = 1
@@ -246,7 +251,7 @@ def run_ours(args):
     # receive it) from pinned host memory, run the step, and read back the interior
     # u, v, w, p that the reference's per-step output routines consume (main.f95:311-327)
     e2e_steps = max(3, min(args.steps, 20))
-    zbm, uin, vin, win = lesgpu.generate_scenario(scenario(seed=1 + rank))
+    zbm, uin, vin, win = lesgpu.generate_scenario(scenario(seed=1 + rank, im=IM, jm=JM, km=KM))
     pin = [torch.from_numpy(np.asfortranarray(a).ravel(order="F").copy()).pin_memory() for a in (uin, vin, win)]
     outs = [torch.empty((KM, JM, IM), dtype=torch.float32).pin_memory() for _ in range(4)]
     lbi, ubi = (1, 1, 0), (JM, KM, 0)
@@ -288,16 +293,17 @@ def run_ours(args):
     line = None
     if rank == 0:
         cpu = None
-        try:
-            cv, sample = cpu_baseline_sample(threads=1)
-            cpu = {"value": cv, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample}
-        except Exception as e:  # the baseline must not sink the GPU line
-            cpu = {"value": None, "unit": UNIT, "cores": 1, "kind": "port", "sample": f"failed: {e}"}
+        if not args.no_cpu:
+            try:
+                cv, sample = cpu_baseline_sample(threads=1)
+                cpu = {"value": cv, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample}
+            except Exception as e:  # the baseline must not sink the GPU line
+                cpu = {"value": None, "unit": UNIT, "cores": 1, "kind": "port", "sample": f"failed: {e}"}
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic: seeded urban heightmap and power-law inflow (no dataset in the reference)",
-                "config": workload_config(), "clocks": clk.summary(),
+                "config": workload_config(IM, JM, KM), "clocks": clk.summary(),
                 "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                         "steps": e2e_steps},
                 "gpu_launches": launches, "nonfinite": bad, "roofline": roofline, "cpu_baseline": cpu}
@@ -314,7 +320,10 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--dims", default=f"{IM}x{JM}x{KM}", help="domain IMxJMxKM (default: the workload's)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     args = ap.parse_args()
+    args.dims = tuple(int(x) for x in args.dims.lower().split("x"))
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -93,7 +93,7 @@ typedef struct les_params {
   float omega, pjuge;   /* SOR relaxation and tolerance, press.f95:43-45         */
   int nmaxp;            /* SOR iteration cap, press.f95:44 (50)                  */
   int sor_fixed;        /* 1: always nmaxp iterations; 0: exit on sor < pjuge     */
-  int sor_depth;        /* SOR iterations fused per pass: 0 = autotuned, 1..4     */
+  int sor_depth;        /* reserved: pass 0                                       */
 } les_params;
 
 /* Synthetic urban scenario (the configs' generator; replaces the GIS inputs read
