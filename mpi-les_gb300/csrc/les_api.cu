@@ -211,7 +211,8 @@ extern "C" int les_gpu_create(const les_dims *dims, const les_params *params, le
   {
     const long long fused = (long long)((im + 31) / 32) * ((jm + 1) / 2) * ((km + 3) / 4);
     const long long inter = (long long)((im + 63) / 64) * ((jm + 3) / 4) * km;
-    h->fix_len = 2 + (size_t)std::max(fused, inter);
+    const long long march = (long long)((im + 31) / 32) * ((jm + 7) / 8) * km;  // les k-march: tile planes
+    h->fix_len = 2 + (size_t)std::max({fused, inter, march});
   }
   if (cudaMalloc(&h->fix_d, FIX_COUNT * h->fix_len * sizeof(int)) != cudaSuccess) {
     (void)cudaGetLastError();

@@ -218,6 +218,14 @@ __device__ __forceinline__ void velfg_block(const LesDom &d, int bx, int by, int
   const bool in = (i0 <= d.im && j0 <= d.jm && k0 <= d.km);
   const int i = min(i0, d.im), j = min(j0, d.jm), k = min(k0, d.km);
   const int c = lix(d, i, j, k);
+  // feedbf operands loaded up front: their latency hides behind the velfg arithmetic
+  uint8_t m = 0;
+  float u = 0.f, v = 0.f, w = 0.f, su = 0.f, sv = 0.f, sw = 0.f;
+  if (FB) {
+    m = d.mask[c];
+    u = d.u[c]; v = d.v[c]; w = d.w[c];
+    su = d.usum[c]; sv = d.vsum[c]; sw = d.wsum[c];
+  }
   VelfgOut o;
   unsigned bd = 0;
   velfg_cell<P2, ZF>(d, i, j, k, c, o, bd);
@@ -238,12 +246,10 @@ __device__ __forceinline__ void velfg_block(const LesDom &d, int bx, int by, int
   }
   float fv = o.f, gv = o.g, hv = o.h;
   if (FB) {  // feedbf.f95:35-61
-    const uint8_t m = d.mask[c];
     const float bm = (m & 1) ? 1.f : 0.f, cm = (m & 2) ? 1.f : 0.f, dm = (m & 4) ? 1.f : 0.f;
-    const float u = d.u[c], v = d.v[c], w = d.w[c];
-    const float us = (d.usum[c] + u) * bm;
-    const float vs = (d.vsum[c] + v) * cm;
-    const float ws = (d.wsum[c] + w) * dm;
+    const float us = (su + u) * bm;
+    const float vs = (sv + v) * cm;
+    const float ws = (sw + w) * dm;
     d.usum[c] = us; d.vsum[c] = vs; d.wsum[c] = ws;
     fv = fv + (d.alpha * us * d.dt + d.beta * u * bm);
     gv = gv + (d.alpha * vs * d.dt + d.beta * v * cm);
@@ -323,125 +329,164 @@ __global__ void __launch_bounds__(FX *FY *FZ) k_les_sm3(LesDom d) {
 }
 
 // ------------------------------------------------------------------ les.f95:83-242
-// The viscous terms of one cell added to f, g, h; gradients from the stored diu, wall
-// ratios from k_wall.
+// The viscous terms of one cell added to f, g, h.  visc_compute is the arithmetic on
+// gathered inputs; visc_cell gathers them from global memory (the fixup path), the
+// k-march kernel below gathers them from its shared-memory planes.  Both run the same
+// FP32 operations, so their results are identical.
+
+// the stencil values one cell reads: sm (s_*), diu as les reads it (g<n>*), f, g, h
+struct ViscIn {
+  float s_c, s_e, s_w, s_n, s_s, s_ne, s_se, s_nw, s_u, s_eu, s_wu, s_nu, s_su, s_d, s_ed;
+  float g1c, g1e, g2c, g2n, g2wn, g3c, g3u, g3wu, g4c, g4e, g4es, g5c, g5n;
+  float g6c, g6u, g6su, g7c, g7e, g7ed, g8c, g8n, g8nd, g9c, g9u;
+  float f0, g0, h0;
+  float ru, rv;  // u/uspd, v/vspd at k = 1 (k_wall)
+};
+// column constants: spacings around (i, j), their neighbour sums, reciprocals
+struct ViscCol {
+  float dx1m, dx1c, dx1p, sxm, sxc, rsxm, rsxc, dxs, rdxs, rdx1;
+  float dy1m, dy1c, dy1p, sym, syc, rsym, rsyc, dys, rdys, rdy1;
+};
+// plane constants at k
+struct ViscZ {
+  float dznm, dznc, dznp, rdznc, rsumc, rsumm;
+};
+__device__ __forceinline__ ViscCol visc_col(const LesDom &d, int i, int j) {
+  const LesGrid1 &g = d.gr;
+  ViscCol c;
+  c.dx1m = g.dx1[i - 1]; c.dx1c = g.dx1[i]; c.dx1p = g.dx1[i + 1];
+  c.sxm = c.dx1m + c.dx1c; c.sxc = c.dx1c + c.dx1p; c.rsxm = g.rdx1s[i - 1]; c.rsxc = g.rdx1s[i];
+  c.dxs = g.dxs[i]; c.rdxs = g.rdxs[i]; c.rdx1 = g.rdx1[i];
+  c.dy1m = g.dy1[j - 1]; c.dy1c = g.dy1[j]; c.dy1p = g.dy1[j + 1];
+  c.sym = c.dy1m + c.dy1c; c.syc = c.dy1c + c.dy1p; c.rsym = g.rdy1s[j - 1]; c.rsyc = g.rdy1s[j];
+  c.dys = g.dys[j]; c.rdys = g.rdys[j]; c.rdy1 = g.rdy1[j];
+  return c;
+}
+__device__ __forceinline__ ViscZ visc_z(const LesDom &d, int k) {
+  const LesGrid1 &g = d.gr;
+  ViscZ z;
+  z.dznm = g.dzn[k - 1]; z.dznc = g.dzn[k]; z.dznp = g.dzn[k + 1];
+  z.rdznc = g.rdzn[k]; z.rsumc = g.rdzsum[k]; z.rsumm = g.rdzsum[k - 1];
+  return z;
+}
+
 template <bool P2, bool ZF>
-__device__ __forceinline__ void visc_cell(const LesDom &d, int i, int j, int k, int c, float &fv, float &gv, float &hv,
-                                          unsigned &bd) {
-  const float *dzn = d.gr.dzn, *rdzn = d.gr.rdzn, *rdzsum = d.gr.rdzsum;
-  const float *dx1 = d.gr.dx1, *dy1 = d.gr.dy1, *dxs = d.gr.dxs, *dys = d.gr.dys;
-  const float *rdx1 = d.gr.rdx1, *rdy1 = d.gr.rdy1, *rdxs = d.gr.rdxs, *rdys = d.gr.rdys;
-  const float s_c = SM_(i, j, k), s_e = SM_(i + 1, j, k), s_w = SM_(i - 1, j, k);
-  const float s_n = SM_(i, j + 1, k), s_s = SM_(i, j - 1, k);
-  const float s_ne = SM_(i + 1, j + 1, k), s_se = SM_(i + 1, j - 1, k), s_nw = SM_(i - 1, j + 1, k);
-  const float s_u = SM_(i, j, k + 1), s_eu = SM_(i + 1, j, k + 1), s_wu = SM_(i - 1, j, k + 1);
-  const float s_nu = SM_(i, j + 1, k + 1), s_su = SM_(i, j - 1, k + 1);
-  const float s_d = SM_(i, j, k - 1), s_ed = SM_(i + 1, j, k - 1);  // plane k-1 (unused at k = 1)
-  // gradients around the cell
-  const float g1c = e1(d, i, j, k), g1e = e1(d, i + 1, j, k);
-  const float g2c = e2(d, i, j, k), g2n = e2(d, i, j + 1, k), g2wn = e2(d, i - 1, j + 1, k);
-  const float g3c = e3(d, i, j, k), g3u = e3(d, i, j, k + 1), g3wu = e3(d, i - 1, j, k + 1);
-  const float g4c = e4(d, i, j, k), g4e = e4(d, i + 1, j, k), g4es = e4(d, i + 1, j - 1, k);
-  const float g5c = e5(d, i, j, k), g5n = e5(d, i, j + 1, k);
-  const float g6c = e6(d, i, j, k), g6u = e6(d, i, j, k + 1), g6su = e6(d, i, j - 1, k + 1);
-  const float g7c = e7(d, i, j, k), g7e = e7(d, i + 1, j, k), g7ed = e7(d, i + 1, j, k - 1);
-  const float g8c = e8(d, i, j, k), g8n = e8(d, i, j + 1, k), g8nd = e8(d, i, j + 1, k - 1);
-  const float g9c = e9(d, i, j, k), g9u = e9(d, i, j, k + 1);
-  const float f0 = d.f[c], g0 = d.g[c], h0 = d.h[c];
-  const float xc = ix_<P2, ZF>(d, i, s_c, s_e, bd);
-  const float xu = ix_<P2, ZF>(d, i, s_u, s_eu, bd);
+__device__ __forceinline__ void visc_compute(const LesDom &d, const ViscIn &v, const ViscCol &cc, const ViscZ &z,
+                                             int k, float &fv, float &gv, float &hv, unsigned &bd) {
+  // (dx1(i+1)*a + dx1(i)*b)/(dx1(i)+dx1(i+1)) and the shifted / y forms of les.f95
+  auto ix = [&](float a, float b) { return dvs<P2, ZF>(cc.dx1p * a + cc.dx1c * b, cc.sxc, cc.rsxc, bd); };
+  auto ixm = [&](float a, float b) { return dvs<P2, ZF>(cc.dx1c * a + cc.dx1m * b, cc.sxm, cc.rsxm, bd); };
+  auto jy = [&](float a, float b) { return dvs<P2, ZF>(cc.dy1p * a + cc.dy1c * b, cc.syc, cc.rsyc, bd); };
+  auto jym = [&](float a, float b) { return dvs<P2, ZF>(cc.dy1c * a + cc.dy1m * b, cc.sym, cc.rsym, bd); };
+  const float xc = ix(v.s_c, v.s_e);
+  const float xu = ix(v.s_u, v.s_eu);
   // x component
   {
-    const float evsx2 = s_e, evsx1 = s_c;
-    const float evsy2 = jy_<P2, ZF>(d, j, xc, ix_<P2, ZF>(d, i, s_n, s_ne, bd), bd);
-    const float evsy1 = jy_<P2, ZF>(d, j, ix_<P2, ZF>(d, i, s_s, s_se, bd), xc, bd);
-    const float visux2 = (evsx2) * 2.f * g1e;
-    const float visux1 = (evsx1) * 2.f * g1c;
-    const float visuy2 = (evsy2) * (g2n + g4e);
-    const float visuy1 = (evsy1) * (g2c + g4es);
+    const float evsx2 = v.s_e, evsx1 = v.s_c;
+    const float evsy2 = jy(xc, ix(v.s_n, v.s_ne));
+    const float evsy1 = jy(ix(v.s_s, v.s_se), xc);
+    const float visux2 = (evsx2) * 2.f * v.g1e;
+    const float visux1 = (evsx1) * 2.f * v.g1c;
+    const float visuy2 = (evsy2) * (v.g2n + v.g4e);
+    const float visuy1 = (evsy1) * (v.g2c + v.g4es);
     float vfu;
     if (k >= 2) {
-      const float evsz2 = dvz<ZF>(dzn[k + 1] * xc + dzn[k] * xu, dzn[k] + dzn[k + 1], rdzsum[k], bd);
-      const float evsz1 = dvz<ZF>(dzn[k] * ix_<P2, ZF>(d, i, s_d, s_ed, bd) + dzn[k - 1] * xc, dzn[k - 1] + dzn[k], rdzsum[k - 1], bd);
-      const float visuz2 = (evsz2) * (g3u + g7e);
-      const float visuz1 = (evsz1) * (g3c + g7ed);
-      vfu = dvs<P2, ZF>(visux2 - visux1, dxs[i], rdxs[i], bd) + dvs<P2, ZF>(visuy2 - visuy1, dy1[j], rdy1[j], bd) +
-            dvz<ZF>(visuz2 - visuz1, dzn[k], rdzn[k], bd);
-    } else {  // les.f95:118-139: the y and z terms appear twice, as written
-      const float evsz2 = dvz<ZF>(dzn[2] * xc + dzn[1] * xu, dzn[1] + dzn[2], rdzsum[1], bd);
-      const float visuz2 = (evsz2) * (g3u + g7e);
-      const float r = __ldg(&d.ruspd[(j + LES_JOFF) * d.pi + i + LES_IOFF]);
-      const float t = dvz<ZF>(0.4f * r, d.logz, d.rlogz, bd);
-      const float visuz1 = t * t * r;
-      const float ty = dvs<P2, ZF>(visuy2 - visuy1, dy1[j], rdy1[j], bd);
-      const float tz = dvz<ZF>(visuz2 - visuz1, dzn[1], rdzn[1], bd);
-      vfu = dvs<P2, ZF>(visux2 - visux1, dxs[i], rdxs[i], bd) + ty + tz + ty + tz;
+      const float evsz2 = dvz<ZF>(z.dznp * xc + z.dznc * xu, z.dznc + z.dznp, z.rsumc, bd);
+      const float evsz1 = dvz<ZF>(z.dznc * ix(v.s_d, v.s_ed) + z.dznm * xc, z.dznm + z.dznc, z.rsumm, bd);
+      const float visuz2 = (evsz2) * (v.g3u + v.g7e);
+      const float visuz1 = (evsz1) * (v.g3c + v.g7ed);
+      vfu = dvs<P2, ZF>(visux2 - visux1, cc.dxs, cc.rdxs, bd) + dvs<P2, ZF>(visuy2 - visuy1, cc.dy1c, cc.rdy1, bd) +
+            dvz<ZF>(visuz2 - visuz1, z.dznc, z.rdznc, bd);
+    } else {  // les.f95:118-139: the y and z terms appear twice, as written (k = 1: dznc = dzn(1))
+      const float evsz2 = dvz<ZF>(z.dznp * xc + z.dznc * xu, z.dznc + z.dznp, z.rsumc, bd);
+      const float visuz2 = (evsz2) * (v.g3u + v.g7e);
+      const float t = dvz<ZF>(0.4f * v.ru, d.logz, d.rlogz, bd);
+      const float visuz1 = t * t * v.ru;
+      const float ty = dvs<P2, ZF>(visuy2 - visuy1, cc.dy1c, cc.rdy1, bd);
+      const float tz = dvz<ZF>(visuz2 - visuz1, z.dznc, z.rdznc, bd);
+      vfu = dvs<P2, ZF>(visux2 - visux1, cc.dxs, cc.rdxs, bd) + ty + tz + ty + tz;
     }
-    fv = f0 + vfu;
+    fv = v.f0 + vfu;
   }
   // y component
   {
-    const float evsy2 = s_n, evsy1 = s_c;
-    const float evsx2 = jy_<P2, ZF>(d, j, xc, ix_<P2, ZF>(d, i, s_n, s_ne, bd), bd);
-    const float evsx1 = jy_<P2, ZF>(d, j, ixm_<P2, ZF>(d, i, s_w, s_c, bd), ixm_<P2, ZF>(d, i, s_nw, s_n, bd), bd);
-    const float visvx2 = (evsx2) * (g2n + g4e);
-    const float visvx1 = (evsx1) * (g2wn + g4c);
-    const float visvy2 = (evsy2) * 2.f * g5n;
-    const float visvy1 = (evsy1) * 2.f * g5c;
+    const float evsy2 = v.s_n, evsy1 = v.s_c;
+    const float evsx2 = jy(xc, ix(v.s_n, v.s_ne));
+    const float evsx1 = jy(ixm(v.s_w, v.s_c), ixm(v.s_nw, v.s_n));
+    const float visvx2 = (evsx2) * (v.g2n + v.g4e);
+    const float visvx1 = (evsx1) * (v.g2wn + v.g4c);
+    const float visvy2 = (evsy2) * 2.f * v.g5n;
+    const float visvy1 = (evsy1) * 2.f * v.g5c;
     float vfv;
     if (k >= 2) {
-      const float evsz2 = dvz<ZF>(dzn[k + 1] * xc + dzn[k] * xu, dzn[k] + dzn[k + 1], rdzsum[k], bd);
-      const float evsz1 = dvz<ZF>(dzn[k] * ix_<P2, ZF>(d, i, s_d, s_ed, bd) + dzn[k - 1] * xc, dzn[k - 1] + dzn[k], rdzsum[k - 1], bd);
-      const float visvz2 = (evsz2) * (g6u + g8n);
-      const float visvz1 = (evsz1) * (g6c + g8nd);
-      vfv = dvs<P2, ZF>(visvx2 - visvx1, dx1[i], rdx1[i], bd) + dvs<P2, ZF>(visvy2 - visvy1, dys[j], rdys[j], bd) +
-            dvz<ZF>(visvz2 - visvz1, dzn[k], rdzn[k], bd);
+      const float evsz2 = dvz<ZF>(z.dznp * xc + z.dznc * xu, z.dznc + z.dznp, z.rsumc, bd);
+      const float evsz1 = dvz<ZF>(z.dznc * ix(v.s_d, v.s_ed) + z.dznm * xc, z.dznm + z.dznc, z.rsumm, bd);
+      const float visvz2 = (evsz2) * (v.g6u + v.g8n);
+      const float visvz1 = (evsz1) * (v.g6c + v.g8nd);
+      vfv = dvs<P2, ZF>(visvx2 - visvx1, cc.dx1c, cc.rdx1, bd) + dvs<P2, ZF>(visvy2 - visvy1, cc.dys, cc.rdys, bd) +
+            dvz<ZF>(visvz2 - visvz1, z.dznc, z.rdznc, bd);
     } else {  // les.f95:178-201
-      const float evsz2 = dvz<ZF>(dzn[2] * xc + dzn[1] * xu, dzn[1] + dzn[2], rdzsum[1], bd);
-      const float visvz2 = (evsz2) * (g6u + g8n);
-      const float r = __ldg(&d.rvspd[(j + LES_JOFF) * d.pi + i + LES_IOFF]);
-      const float t = dvz<ZF>(0.4f * r, d.logz, d.rlogz, bd);
-      const float visvz1 = t * t * r;
-      vfv = dvs<P2, ZF>(visvx2 - visvx1, dx1[i], rdx1[i], bd) + dvs<P2, ZF>(visvy2 - visvy1, dys[j], rdys[j], bd) +
-            dvz<ZF>(visvz2 - visvz1, dzn[1], rdzn[1], bd);
+      const float evsz2 = dvz<ZF>(z.dznp * xc + z.dznc * xu, z.dznc + z.dznp, z.rsumc, bd);
+      const float visvz2 = (evsz2) * (v.g6u + v.g8n);
+      const float t = dvz<ZF>(0.4f * v.rv, d.logz, d.rlogz, bd);
+      const float visvz1 = t * t * v.rv;
+      vfv = dvs<P2, ZF>(visvx2 - visvx1, cc.dx1c, cc.rdx1, bd) + dvs<P2, ZF>(visvy2 - visvy1, cc.dys, cc.rdys, bd) +
+            dvz<ZF>(visvz2 - visvz1, z.dznc, z.rdznc, bd);
     }
-    gv = g0 + vfv;
+    gv = v.g0 + vfv;
   }
   // z component, k = 1..km
   {
-    const float dzc = dzn[k] + dzn[k + 1], rdzc = rdzsum[k];
-    const float evsz2 = s_u, evsz1 = s_c;
-    const float evsx2 = dvz<ZF>(dzn[k + 1] * xc + dzn[k] * xu, dzc, rdzc, bd);
-    const float evsx1 = dvz<ZF>(dzn[k + 1] * ixm_<P2, ZF>(d, i, s_w, s_c, bd) + dzn[k] * ixm_<P2, ZF>(d, i, s_wu, s_u, bd), dzc, rdzc, bd);
-    const float evsy2 = dvz<ZF>(dzn[k + 1] * jy_<P2, ZF>(d, j, s_c, s_n, bd) + dzn[k] * jy_<P2, ZF>(d, j, s_u, s_nu, bd), dzc, rdzc, bd);
-    const float evsy1 = dvz<ZF>(dzn[k + 1] * jym_<P2, ZF>(d, j, s_s, s_c, bd) + dzn[k] * jym_<P2, ZF>(d, j, s_su, s_u, bd), dzc, rdzc, bd);
-    const float viswx2 = (evsx2) * (g3u + g7e);
-    const float viswx1 = (evsx1) * (g3wu + g7c);
-    const float viswy2 = (evsy2) * (g6u + g8n);
-    const float viswy1 = (evsy1) * (g6su + g8c);
-    const float viswz2 = (evsz2) * 2.f * g9u;
-    const float viswz1 = (evsz1) * 2.f * g9c;
-    const float vfw = dvs<P2, ZF>(viswx2 - viswx1, dx1[i], rdx1[i], bd) + dvs<P2, ZF>(viswy2 - viswy1, dy1[j], rdy1[j], bd) +
-                      dvz<ZF>(viswz2 - viswz1, dzn[k], rdzn[k], bd);
-    hv = h0 + vfw;
+    const float dzc = z.dznc + z.dznp, rdzc = z.rsumc;
+    const float evsz2 = v.s_u, evsz1 = v.s_c;
+    const float evsx2 = dvz<ZF>(z.dznp * xc + z.dznc * xu, dzc, rdzc, bd);
+    const float evsx1 = dvz<ZF>(z.dznp * ixm(v.s_w, v.s_c) + z.dznc * ixm(v.s_wu, v.s_u), dzc, rdzc, bd);
+    const float evsy2 = dvz<ZF>(z.dznp * jy(v.s_c, v.s_n) + z.dznc * jy(v.s_u, v.s_nu), dzc, rdzc, bd);
+    const float evsy1 = dvz<ZF>(z.dznp * jym(v.s_s, v.s_c) + z.dznc * jym(v.s_su, v.s_u), dzc, rdzc, bd);
+    const float viswx2 = (evsx2) * (v.g3u + v.g7e);
+    const float viswx1 = (evsx1) * (v.g3wu + v.g7c);
+    const float viswy2 = (evsy2) * (v.g6u + v.g8n);
+    const float viswy1 = (evsy1) * (v.g6su + v.g8c);
+    const float viswz2 = (evsz2) * 2.f * v.g9u;
+    const float viswz1 = (evsz1) * 2.f * v.g9c;
+    const float vfw = dvs<P2, ZF>(viswx2 - viswx1, cc.dx1c, cc.rdx1, bd) + dvs<P2, ZF>(viswy2 - viswy1, cc.dy1c, cc.rdy1, bd) +
+                      dvz<ZF>(viswz2 - viswz1, z.dznc, z.rdznc, bd);
+    hv = v.h0 + vfw;
   }
 }
 
-// les viscous terms (+ adam.f95:30-44 when AD) of the block (bx, by, bz); ZF as in
-// velfg_block.
-template <bool P2, bool ZF, bool AD>
-__device__ __forceinline__ void visc_block(const LesDom &d, int bx, int by, int bz) {
-  const int i0 = bx * FX + threadIdx.x + 1, j0 = by * FY + threadIdx.y + 1, k0 = bz * FZ + threadIdx.z + 1;
-  const bool in = (i0 <= d.im && j0 <= d.jm && k0 <= d.km);
-  const int i = min(i0, d.im), j = min(j0, d.jm), k = min(k0, d.km);
-  const int c = lix(d, i, j, k);
-  float fv, gv, hv;
-  unsigned bd = 0;
-  visc_cell<P2, ZF>(d, i, j, k, c, fv, gv, hv, bd);
-  if (ZF && defer_block(bd, d.fix[FIX_VISC])) return;
-  if (!in) return;
-  if (AD) {  // adam.f95:30-44
-    const float fo = d.fold[c], go = d.gold[c], ho = d.hold[c];
+// gradients and sm around (i, j, k) from global memory
+template <bool P2, bool ZF>
+__device__ __forceinline__ void visc_cell(const LesDom &d, int i, int j, int k, int c, float &fv, float &gv, float &hv,
+                                          unsigned &bd) {
+  ViscIn v;
+  v.s_c = SM_(i, j, k); v.s_e = SM_(i + 1, j, k); v.s_w = SM_(i - 1, j, k);
+  v.s_n = SM_(i, j + 1, k); v.s_s = SM_(i, j - 1, k);
+  v.s_ne = SM_(i + 1, j + 1, k); v.s_se = SM_(i + 1, j - 1, k); v.s_nw = SM_(i - 1, j + 1, k);
+  v.s_u = SM_(i, j, k + 1); v.s_eu = SM_(i + 1, j, k + 1); v.s_wu = SM_(i - 1, j, k + 1);
+  v.s_nu = SM_(i, j + 1, k + 1); v.s_su = SM_(i, j - 1, k + 1);
+  v.s_d = SM_(i, j, k - 1); v.s_ed = SM_(i + 1, j, k - 1);
+  v.g1c = e1(d, i, j, k); v.g1e = e1(d, i + 1, j, k);
+  v.g2c = e2(d, i, j, k); v.g2n = e2(d, i, j + 1, k); v.g2wn = e2(d, i - 1, j + 1, k);
+  v.g3c = e3(d, i, j, k); v.g3u = e3(d, i, j, k + 1); v.g3wu = e3(d, i - 1, j, k + 1);
+  v.g4c = e4(d, i, j, k); v.g4e = e4(d, i + 1, j, k); v.g4es = e4(d, i + 1, j - 1, k);
+  v.g5c = e5(d, i, j, k); v.g5n = e5(d, i, j + 1, k);
+  v.g6c = e6(d, i, j, k); v.g6u = e6(d, i, j, k + 1); v.g6su = e6(d, i, j - 1, k + 1);
+  v.g7c = e7(d, i, j, k); v.g7e = e7(d, i + 1, j, k); v.g7ed = e7(d, i + 1, j, k - 1);
+  v.g8c = e8(d, i, j, k); v.g8n = e8(d, i, j + 1, k); v.g8nd = e8(d, i, j + 1, k - 1);
+  v.g9c = e9(d, i, j, k); v.g9u = e9(d, i, j, k + 1);
+  v.f0 = d.f[c]; v.g0 = d.g[c]; v.h0 = d.h[c];
+  v.ru = (k == 1) ? __ldg(&d.ruspd[(j + LES_JOFF) * d.pi + i + LES_IOFF]) : 0.f;
+  v.rv = (k == 1) ? __ldg(&d.rvspd[(j + LES_JOFF) * d.pi + i + LES_IOFF]) : 0.f;
+  visc_compute<P2, ZF>(d, v, visc_col(d, i, j), visc_z(d, k), k, fv, gv, hv, bd);
+}
+
+// adam.f95:30-44 (when AD; fo, go, ho: fold, gold, hold loaded by the caller ahead of
+// time, so their latency hides behind the viscous arithmetic) and the stores of one cell
+template <bool AD>
+__device__ __forceinline__ void visc_store(const LesDom &d, int c, float fv, float gv, float hv, float fo, float go,
+                                           float ho) {
+  if (AD) {
     d.fold[c] = fv; d.gold[c] = gv; d.hold[c] = hv;
     fv = 1.5f * fv - 0.5f * fo;
     gv = 1.5f * gv - 0.5f * go;
@@ -451,13 +496,191 @@ __device__ __forceinline__ void visc_block(const LesDom &d, int bx, int by, int 
   d.g[c] = gv;
   d.h[c] = hv;
 }
-template <bool P2, bool ZF, bool AD>
-__global__ void __launch_bounds__(FX *FY *FZ) k_les_visc3(LesDom d) {
-  visc_block<P2, ZF, AD>(d, blockIdx.x, blockIdx.y, blockIdx.z);
+
+// ---- the k-march kernel ------------------------------------------------------------
+// A block owns a VTX x VTY tile of columns and marches k over a chunk of VKC planes.
+// The planes of sm and diu1..9 that a cell reads (as les reads them: index remaps and
+// zero entries applied at load time) sit in a shared-memory ring with a one-cell halo;
+// each step's new planes are loaded into registers while the current plane computes.
+constexpr int VTX = 32, VTY = 8, VTW = VTX + 2, VTH = VTY + 2, VTN = VTW * VTH, VKC = 30;
+constexpr int VEL = (VTN + VTX * VTY - 1) / (VTX * VTY);  // tile elements per thread (2)
+// ring slots: sm 3 planes; diu1, 2, 4, 5 one; diu3, 6, 9 (k, k+1) and diu7, 8 (k-1, k) two
+enum { S_SM = 0, S_E1 = 3, S_E2, S_E4, S_E5, S_E3 = 7, S_E6 = 9, S_E9 = 11, S_E7 = 13, S_E8 = 15, S_N = 17 };
+
+// value of array q (0 = sm, n = diu_n as les reads it) at tile point (ii, jj, kk);
+// points past the domain edge are clamped into the allocation (never used)
+__device__ __forceinline__ float visc_src(const LesDom &d, int q, int ii, int jj, int kk) {
+  ii = min(ii, d.im + 2);
+  jj = min(jj, d.jm + 2);
+  const int iA = min(ii, d.im), jP = (jj > d.jm) ? 1 : jj, jM = (jj <= 0) ? d.jm : jj;
+  const bool kz7 = (kk <= 0 || kk >= d.km);
+  switch (q) {
+    case 0: return SM_(ii, jj, kk);
+    case 1: return DIU_(1, iA, jj, kk);
+    case 2: return (ii <= 0) ? 0.f : DIU_(2, ii, jP, kk);
+    case 3: return (ii <= 0) ? 0.f : DIU_(3, ii, jj, kk);
+    case 4: return DIU_(4, iA, jM, kk);
+    case 5: return DIU_(5, ii, jP, kk);
+    case 6: return DIU_(6, ii, jM, kk);
+    case 7: return kz7 ? 0.f : DIU_(7, iA, jj, kk);
+    case 8: return kz7 ? 0.f : DIU_(8, ii, jP, kk);
+    default: return (kk > d.km) ? 0.f : DIU_(9, ii, jj, kk);
+  }
 }
+
+template <bool P2, bool ZF, bool AD>
+__global__ void __launch_bounds__(VTX *VTY, 2) k_les_visc_march(LesDom d) {
+  __shared__ float ring[S_N * VTN];
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * VTX + tx;
+  const int i0 = blockIdx.x * VTX, j0 = blockIdx.y * VTY;  // tile origin (halo) at (i0, j0)
+  const int k0 = blockIdx.z * VKC + 1, k1 = min(k0 + VKC - 1, d.km);
+  const int i = i0 + tx + 1, j = j0 + ty + 1;
+  const bool in = (i <= d.im && j <= d.jm);
+  const int ic = min(i, d.im), jc = min(j, d.jm);
+  // this thread's tile elements
+  int ea[VEL], eb[VEL];
+  bool ev[VEL];
+#pragma unroll
+  for (int q = 0; q < VEL; ++q) {
+    const int e = tid + q * VTX * VTY;
+    ev[q] = e < VTN;
+    ea[q] = e % VTW;
+    eb[q] = e / VTW;
+  }
+  auto put = [&](int slot, int q, int kk) {  // load one plane of array q into `slot` (synchronous)
+#pragma unroll
+    for (int t = 0; t < VEL; ++t)
+      if (ev[t]) ring[slot * VTN + eb[t] * VTW + ea[t]] = visc_src(d, q, i0 + ea[t], j0 + eb[t], kk);
+  };
+  // prologue: the planes step k0 reads
+  put(S_SM + (k0 - 1) % 3, 0, k0 - 1);
+  put(S_SM + k0 % 3, 0, k0);
+  put(S_SM + (k0 + 1) % 3, 0, k0 + 1);
+  put(S_E1, 1, k0); put(S_E2, 2, k0); put(S_E4, 4, k0); put(S_E5, 5, k0);
+  put(S_E3 + (k0 & 1), 3, k0); put(S_E3 + ((k0 + 1) & 1), 3, k0 + 1);
+  put(S_E6 + (k0 & 1), 6, k0); put(S_E6 + ((k0 + 1) & 1), 6, k0 + 1);
+  put(S_E9 + (k0 & 1), 9, k0); put(S_E9 + ((k0 + 1) & 1), 9, k0 + 1);
+  put(S_E7 + ((k0 - 1) & 1), 7, k0 - 1); put(S_E7 + (k0 & 1), 7, k0);
+  put(S_E8 + ((k0 - 1) & 1), 8, k0 - 1); put(S_E8 + (k0 & 1), 8, k0);
+  const ViscCol cc = visc_col(d, ic, jc);
+  float ru = 0.f, rv = 0.f;
+  if (k0 == 1) {
+    ru = __ldg(&d.ruspd[(jc + LES_JOFF) * d.pi + ic + LES_IOFF]);
+    rv = __ldg(&d.rvspd[(jc + LES_JOFF) * d.pi + ic + LES_IOFF]);
+  }
+  int c = lix(d, ic, jc, k0);
+  float f0 = d.f[c], g0 = d.g[c], h0 = d.h[c];
+  float fo = 0.f, go = 0.f, ho = 0.f;
+  if (AD) { fo = d.fold[c]; go = d.gold[c]; ho = d.hold[c]; }
+  __syncthreads();
+  const int a = tx + 1, b = ty + 1;
+#define RS(slot, da, db) ring[(slot) * VTN + (b + (db)) * VTW + (a + (da))]
+  for (int k = k0; k <= k1; ++k) {
+    const bool more = k < k1;
+    // next step's planes and cell values, in flight while this plane computes
+    float nx[10][VEL];
+    float nf = 0.f, ng = 0.f, nh = 0.f, nfo = 0.f, ngo = 0.f, nho = 0.f;
+    if (more) {
+#pragma unroll
+      for (int t = 0; t < VEL; ++t) {
+        if (!ev[t]) continue;
+        const int ii = i0 + ea[t], jj = j0 + eb[t];
+        nx[0][t] = visc_src(d, 0, ii, jj, k + 2);
+        nx[1][t] = visc_src(d, 1, ii, jj, k + 1);
+        nx[2][t] = visc_src(d, 2, ii, jj, k + 1);
+        nx[4][t] = visc_src(d, 4, ii, jj, k + 1);
+        nx[5][t] = visc_src(d, 5, ii, jj, k + 1);
+        nx[3][t] = visc_src(d, 3, ii, jj, k + 2);
+        nx[6][t] = visc_src(d, 6, ii, jj, k + 2);
+        nx[9][t] = visc_src(d, 9, ii, jj, k + 2);
+        nx[7][t] = visc_src(d, 7, ii, jj, k + 1);
+        nx[8][t] = visc_src(d, 8, ii, jj, k + 1);
+      }
+      const int cn = c + d.np;
+      nf = d.f[cn]; ng = d.g[cn]; nh = d.h[cn];
+      if (AD) { nfo = d.fold[cn]; ngo = d.gold[cn]; nho = d.hold[cn]; }
+    }
+    // gather this cell's stencil from the ring
+    const int sm0 = S_SM + (k - 1) % 3, sm1 = S_SM + k % 3, sm2 = S_SM + (k + 1) % 3;
+    const int e3c = S_E3 + (k & 1), e3u = S_E3 + ((k + 1) & 1);
+    const int e6c = S_E6 + (k & 1), e6u = S_E6 + ((k + 1) & 1);
+    const int e9c = S_E9 + (k & 1), e9u = S_E9 + ((k + 1) & 1);
+    const int e7c = S_E7 + (k & 1), e7d = S_E7 + ((k - 1) & 1);
+    const int e8c = S_E8 + (k & 1), e8d = S_E8 + ((k - 1) & 1);
+    ViscIn v;
+    v.s_c = RS(sm1, 0, 0); v.s_e = RS(sm1, 1, 0); v.s_w = RS(sm1, -1, 0);
+    v.s_n = RS(sm1, 0, 1); v.s_s = RS(sm1, 0, -1);
+    v.s_ne = RS(sm1, 1, 1); v.s_se = RS(sm1, 1, -1); v.s_nw = RS(sm1, -1, 1);
+    v.s_u = RS(sm2, 0, 0); v.s_eu = RS(sm2, 1, 0); v.s_wu = RS(sm2, -1, 0);
+    v.s_nu = RS(sm2, 0, 1); v.s_su = RS(sm2, 0, -1);
+    v.s_d = RS(sm0, 0, 0); v.s_ed = RS(sm0, 1, 0);
+    v.g1c = RS(S_E1, 0, 0); v.g1e = RS(S_E1, 1, 0);
+    v.g2c = RS(S_E2, 0, 0); v.g2n = RS(S_E2, 0, 1); v.g2wn = RS(S_E2, -1, 1);
+    v.g3c = RS(e3c, 0, 0); v.g3u = RS(e3u, 0, 0); v.g3wu = RS(e3u, -1, 0);
+    v.g4c = RS(S_E4, 0, 0); v.g4e = RS(S_E4, 1, 0); v.g4es = RS(S_E4, 1, -1);
+    v.g5c = RS(S_E5, 0, 0); v.g5n = RS(S_E5, 0, 1);
+    v.g6c = RS(e6c, 0, 0); v.g6u = RS(e6u, 0, 0); v.g6su = RS(e6u, 0, -1);
+    v.g7c = RS(e7c, 0, 0); v.g7e = RS(e7c, 1, 0); v.g7ed = RS(e7d, 1, 0);
+    v.g8c = RS(e8c, 0, 0); v.g8n = RS(e8c, 0, 1); v.g8nd = RS(e8d, 0, 1);
+    v.g9c = RS(e9c, 0, 0); v.g9u = RS(e9u, 0, 0);
+    v.f0 = f0; v.g0 = g0; v.h0 = h0;
+    v.ru = ru; v.rv = rv;
+    float fv, gv, hv;
+    unsigned bd = 0;
+    visc_compute<P2, ZF>(d, v, cc, visc_z(d, k), k, fv, gv, hv, bd);
+    // every thread is done with the ring; a plane with a deferred cell is stored by the fixup
+    const bool defer = ZF && __syncthreads_or(in ? bd : 0u);
+    if (!ZF) __syncthreads();
+    if (defer) {
+      if (tid == 0) {
+        int *list = d.fix[FIX_VISC];
+        const int s = atomicAdd(list, 1);
+        list[2 + s] = (int)(((k - 1) * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x);
+      }
+    } else if (in) {
+      visc_store<AD>(d, c, fv, gv, hv, fo, go, ho);
+    }
+    if (more) {
+#pragma unroll
+      for (int t = 0; t < VEL; ++t) {
+        if (!ev[t]) continue;
+        const int o = eb[t] * VTW + ea[t];
+        ring[(S_SM + (k + 2) % 3) * VTN + o] = nx[0][t];
+        ring[S_E1 * VTN + o] = nx[1][t];
+        ring[S_E2 * VTN + o] = nx[2][t];
+        ring[S_E4 * VTN + o] = nx[4][t];
+        ring[S_E5 * VTN + o] = nx[5][t];
+        ring[(S_E3 + (k & 1)) * VTN + o] = nx[3][t];
+        ring[(S_E6 + (k & 1)) * VTN + o] = nx[6][t];
+        ring[(S_E9 + (k & 1)) * VTN + o] = nx[9][t];
+        ring[(S_E7 + ((k + 1) & 1)) * VTN + o] = nx[7][t];
+        ring[(S_E8 + ((k + 1) & 1)) * VTN + o] = nx[8][t];
+      }
+      c += d.np;
+      f0 = nf; g0 = ng; h0 = nh;
+      fo = nfo; go = ngo; ho = nho;
+      ru = 0.f; rv = 0.f;
+      __syncthreads();
+    }
+  }
+#undef RS
+}
+
+// deferred planes of k_les_visc_march: entry ((k-1)*gy + by)*gx + bx, recomputed
+// cell by cell with IEEE divisions from global memory
 template <bool P2, bool AD>
-__global__ void __launch_bounds__(FX *FY *FZ) k_les_visc3_fix(LesDom d, uint3 g) {
-  for_deferred(d.fix[FIX_VISC], g, [&](int bx, int by, int bz) { visc_block<P2, false, AD>(d, bx, by, bz); });
+__global__ void __launch_bounds__(VTX *VTY) k_les_visc_fix(LesDom d, uint3 g) {
+  for_deferred(d.fix[FIX_VISC], g, [&](int bx, int by, int bz) {
+    const int i = bx * VTX + (int)threadIdx.x + 1, j = by * VTY + (int)threadIdx.y + 1, k = bz + 1;
+    if (i > d.im || j > d.jm) return;
+    const int c = lix(d, i, j, k);
+    float fv, gv, hv;
+    unsigned bd = 0;
+    float fo = 0.f, go = 0.f, ho = 0.f;
+    if (AD) { fo = d.fold[c]; go = d.gold[c]; ho = d.hold[c]; }
+    visc_cell<P2, false>(d, i, j, k, c, fv, gv, hv, bd);
+    visc_store<AD>(d, c, fv, gv, hv, fo, go, ho);
+  });
 }
 
 inline dim3 fgrid(const LesDom &d) { return dim3((d.im + FX - 1) / FX, (d.jm + FY - 1) / FY, (d.km + FZ - 1) / FZ); }
@@ -474,8 +697,7 @@ namespace {
 // Launch a fused kernel K<P2, ZF, X> for the domain's spacing modes; with ZF its fixup
 // kernel F<P2, X> follows (it does nothing when no block was deferred).
 template <template <bool, bool, bool> class K, template <bool, bool> class F>
-void launch_variant(const LesDom &d, bool x, LesCtx ctx) {
-  const dim3 g = fgrid(d), b(FX, FY, FZ);
+void launch_variant(const LesDom &d, bool x, LesCtx ctx, dim3 g, dim3 b) {
   const uint3 gu = make_uint3(g.x, g.y, g.z);
   const unsigned nfix = std::min<unsigned>(g.x * g.y * g.z, (unsigned)std::max(1, 2 * d.sms));
   const int v = (d.xy_pow2 ? 4 : 0) | (d.zfast ? 2 : 0) | (x ? 1 : 0);
@@ -504,22 +726,24 @@ struct VelfgF {
 };
 template <bool A, bool B, bool C>
 struct ViscK {
-  static constexpr auto fn = k_les_visc3<A, B, C>;
+  static constexpr auto fn = k_les_visc_march<A, B, C>;
 };
 template <bool A, bool C>
 struct ViscF {
-  static constexpr auto fn = k_les_visc3_fix<A, C>;
+  static constexpr auto fn = k_les_visc_fix<A, C>;
 };
 }  // namespace
 
 void les_launch_velfg_fused(const LesDom &d, bool with_feedbf, LesCtx ctx) {
   LAUNCH(ctx, (k_wall<<<dim3((d.im + 127) / 128, d.jm), 128, 0, ctx.s>>>(d)));
-  launch_variant<VelfgK, VelfgF>(d, with_feedbf, ctx);
+  launch_variant<VelfgK, VelfgF>(d, with_feedbf, ctx, fgrid(d), dim3(FX, FY, FZ));
 }
 
 void les_launch_les_fused(const LesDom &d, bool with_adam, LesCtx ctx) {
   const dim3 g = fgrid(d), b(FX, FY, FZ);
   LAUNCH(ctx, k_les_sm3<<<g, b, 0, ctx.s>>>(d));
   les_launch_boundsm(d, ctx);
-  launch_variant<ViscK, ViscF>(d, with_adam, ctx);
+  // the k-march: 32 x 8 column tiles, chunks of VKC planes
+  const dim3 gv((d.im + VTX - 1) / VTX, (d.jm + VTY - 1) / VTY, (d.km + VKC - 1) / VKC);
+  launch_variant<ViscK, ViscF>(d, with_adam, ctx, gv, dim3(VTX, VTY));
 }
