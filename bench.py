@@ -12,6 +12,14 @@ step of the reference's solver loop (velnw .. press).
 --dims runs a smaller domain of the same kind (profiling captures: ncu wants a small
 case); --no-cpu skips the CPU baseline leg.  The headline line uses the defaults.
 
+Besides the headline, the line carries the batched ensembles: "batched" (64 domains of
+150x150x90, each with its own building seed, inflow direction in [0, 360) and speed in
+[2, 10] m/s, stepped together; against one 150x150x90 domain alone) and "uneven" (96
+domains with ip, jp in {64..256}, kp in {48, 64, 90}, coverage 15-45%; against the
+same domains run one by one).  --mode serve runs the serving stream instead (Poisson
+arrivals of such scenarios, 50-500 steps each) and prints its own line with p50/p99
+completion latency and an FP64-oracle check of sampled requests.
+
 One JSON line on stdout (rank 0).  Under torchrun each rank advances its own
 independent domain (replicas; the single domain does not shard without a halo
 exchange), so per-GPU work is fixed as N grows ("scaling": "weak").
@@ -207,6 +215,95 @@ def run_reference(args):
     return 0
 
 
+def _seconds_synced(fn):
+    t0 = time.perf_counter()
+    fn()
+    return time.perf_counter() - t0
+
+
+def ensemble(specs, warmup, steps, params=None):
+    """Step scenarios together in one batch; returns (cell-steps/s, seconds per step).
+    Timed on the host between full device synchronisations (the members run on many
+    streams)."""
+    import lesgpu
+    params = params or lesgpu.Params()
+    doms = []
+    for sc in specs:
+        d = lesgpu.Domain(sc.im, sc.jm, sc.km, params)
+        d.setup_scenario(sc)
+        doms.append(d)
+    b = lesgpu.Batch()
+    for d in doms:
+        b.add(d, 1, 10**6)
+    for _ in range(warmup):
+        b.step()
+    b.sync()
+    dt = _seconds_synced(lambda: ([b.step() for _ in range(steps)], b.sync()))
+    cells = sum(sc.im * sc.jm * sc.km for sc in specs)
+    bad = sum(d.nonfinite() for d in doms)
+    b.close()
+    for d in doms:
+        d.close()
+    return cells * steps / dt, dt / steps, bad
+
+
+def one_by_one(specs, warmup, steps, params=None):
+    """The same scenarios on the plain path, one domain after the other."""
+    import lesgpu
+    params = params or lesgpu.Params()
+    total_t, work = 0.0, 0
+    for sc in specs:
+        d = lesgpu.Domain(sc.im, sc.jm, sc.km, params)
+        d.setup_scenario(sc)
+        for n in range(1, warmup + 1):
+            d.step(n, 10**6)
+        d.sync()
+        total_t += _seconds_synced(lambda: ([d.step(n, 10**6) for n in range(warmup + 1, warmup + steps + 1)],
+                                            d.sync()))
+        work += sc.im * sc.jm * sc.km * steps
+        d.close()
+    return work / total_t
+
+
+def uniform_specs(count=64, seed=2024, im=150, jm=150, km=90):
+    import random
+
+    import lesgpu
+    rng = random.Random(seed)
+    return [lesgpu.Scenario(im=im, jm=jm, km=km, seed=rng.getrandbits(48), direction_deg=rng.uniform(0.0, 360.0),
+                            u_ref=rng.uniform(2.0, 10.0)) for _ in range(count)]
+
+
+def uneven_specs(count=96, seed=2025):
+    import random
+
+    import lesgpu
+    rng = random.Random(seed)
+    sizes, kms = (64, 96, 128, 192, 256), (48, 64, 90)
+    return [lesgpu.Scenario(im=rng.choice(sizes), jm=rng.choice(sizes), km=rng.choice(kms), seed=rng.getrandbits(48),
+                            coverage=rng.uniform(0.15, 0.45), direction_deg=rng.uniform(0.0, 360.0),
+                            u_ref=rng.uniform(2.0, 10.0)) for _ in range(count)]
+
+
+def batched_lines(warmup=3, steps=10):
+    """The two ensemble measurements carried by the headline line."""
+    uni = uniform_specs()
+    v_batch, s_step, bad = ensemble(uni, warmup, steps)
+    v_alone = one_by_one(uni[:1], warmup, steps)
+    batched = {"value": v_batch, "unit": UNIT, "ms_per_step": 1e3 * s_step, "nonfinite": bad,
+               "workload": "64 domains of 150x150x90, own building seed, inflow direction U[0,360), speed U[2,10] m/s",
+               "plain_small_value": v_alone, "vs_plain_small": v_batch / v_alone,
+               "timing": "host clock between device synchronisations, after warm-up"}
+    une = uneven_specs()
+    v_ub, s_ub, bad_u = ensemble(une, warmup, steps)
+    v_obo = one_by_one(une, warmup, 3)
+    uneven = {"value": v_ub, "unit": UNIT, "ms_per_step": 1e3 * s_ub, "nonfinite": bad_u,
+              "workload": "96 domains, ip, jp in {64,96,128,192,256}, kp in {48,64,90}, coverage U[15,45]%",
+              "cells": sum(sc.im * sc.jm * sc.km for sc in une), "one_by_one_value": v_obo,
+              "vs_one_by_one": v_ub / v_obo}
+    return batched, uneven
+
+
 def run_ours(args):
     world, rank, local, pg = dist_setup()
     import numpy as np
@@ -307,6 +404,11 @@ def run_ours(args):
                 "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                         "steps": e2e_steps},
                 "gpu_launches": launches, "nonfinite": bad, "roofline": roofline, "cpu_baseline": cpu}
+        if not args.no_batch:
+            try:
+                line["batched"], line["uneven"] = batched_lines()
+            except Exception as e:  # the ensembles must not sink the headline line
+                line["batched"] = {"failed": str(e)}
         print(json.dumps(line), flush=True)
     if pg is not None:
         pg.barrier()
@@ -314,7 +416,82 @@ def run_ours(args):
     return 0
 
 
+def _oracle_check(job):
+    """FP64 oracle run of one served scenario (runs in a spawned worker process)."""
+    sc_kw, nsteps, gpu_fields = job
+    os.environ.setdefault("OMP_NUM_THREADS", "2")
+    import numpy as np
+
+    import lesgpu
+    from oracle import ref as oref
+    sc = lesgpu.Scenario(**sc_kw)
+    zbm, uin, vin, win = lesgpu.generate_scenario(sc)
+    r = oref.Ref(8, sc.im, sc.jm, sc.km, zbm, uin, vin, win, dx=sc.dx, dy=sc.dy, dz_law=sc.dz_law, dz0=sc.dz0,
+                 dz_ratio=sc.dz_ratio, sqrt_half=0, red64=1, fast=True)
+    for n in range(1, nsteps + 1):
+        r.step(n, nsteps)
+    err = 0.0
+    for fid, g in gpu_fields.items():
+        o = r.get(fid, (1, 1, 1), (sc.im, sc.jm, sc.km))
+        err = max(err, float(np.abs(g.astype(np.float64) - o).max() / max(np.abs(o).max(), 1e-30)))
+    r.close()
+    return err
+
+
+def run_serve(args):
+    """The serving stream: Poisson arrivals, admission by free HBM, continuous batching."""
+    import dataclasses
+    import multiprocessing as mp
+
+    # the oracle workers start before the first GPU call (spawn): the check runs after
+    mp_ctx = mp.get_context("spawn")
+    pool = mp_ctx.Pool(processes=max(1, min(8, (os.cpu_count() or 2) // 2)))
+    import lesgpu
+    import serve
+    if not os.path.exists(lesgpu.LIB_PATH):
+        import __graft_entry__
+        __graft_entry__.build()
+    reqs = serve.poisson_requests(args.rate, args.serve_seconds, seed=7)
+    be = serve.GpuBackend(reserve_bytes=8 << 30)
+    check_steps = 5
+    sampled = [r.rid for r in reqs][::20][:args.check]  # every 20th request (5%), the first --check of them
+    probes = {}
+
+    def on_step(live):
+        for slot, (r, dom) in live.items():
+            if r.rid in sampled and r.rid not in probes:
+                n, _ = be.batch.progress(slot)
+                if n - 1 == check_steps:
+                    dom.sync()
+                    probes[r.rid] = {fid: dom.download(fid, (1, 1, 1), (r.im, r.jm, r.km))
+                                     for fid in (lesgpu.U, lesgpu.V, lesgpu.W, lesgpu.P)}
+
+    srv = serve.Server(be, max_live=256, setup_workers=4, on_step=on_step)
+    with ClockSampler(0) as clk:
+        st = srv.run(reqs)
+    be.batch.close()
+    jobs = [(dataclasses.asdict(be.scenario(r)), check_steps, probes[r.rid]) for r in reqs if r.rid in probes]
+    errs = pool.map(_oracle_check, jobs) if jobs else []
+    pool.close()
+    line = {"metric": METRIC, "mode": "serve", "value": st["cell_steps_per_s"], "unit": UNIT, "n_gpus": 1,
+            "higher_is_better": True, "dtype": "f32", "data": "synthetic Poisson stream of seeded urban scenarios",
+            "config": {"workload": f"serving: Poisson {args.rate} req/s for {args.serve_seconds} s, grids "
+                                   "ip,jp in {64..256}, kp in {48,64,90}, 50-500 steps",
+                       "rate_hz": args.rate, "window_s": args.serve_seconds},
+            "latency_s": st["latency_s"], "queue_wait_s": st["queue_wait_s"], "requests": st["requests"],
+            "completed": st["completed"], "rejected": st["rejected"], "wall_s": st["wall_s"],
+            "max_backlog": st["max_backlog"], "batch_iterations": st["batch_iterations"],
+            "mean_live_cells": st["mean_live_cells"], "clocks": clk.summary(),
+            "oracle_check": {"requests": len(errs), "steps": check_steps, "max_rel_err": max(errs) if errs else None,
+                             "sample": f"every 20th request (5 percent), the first {args.check} of them; u, v, w, "
+                                       f"p after {check_steps} steps vs the FP64 oracle"}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
+    # many streams (batched ensembles): let them overlap; must precede CUDA start-up
+    os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
@@ -322,12 +499,19 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--dims", default=f"{IM}x{JM}x{KM}", help="domain IMxJMxKM (default: the workload's)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-ensemble measurements")
+    ap.add_argument("--mode", default="plain", choices=["plain", "serve"])
+    ap.add_argument("--serve-seconds", type=float, default=120.0, help="serve mode: arrival window")
+    ap.add_argument("--rate", type=float, default=20.0, help="serve mode: requests per second")
+    ap.add_argument("--check", type=int, default=12, help="serve mode: sampled requests checked vs FP64")
     args = ap.parse_args()
     args.dims = tuple(int(x) for x in args.dims.lower().split("x"))
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.mode == "serve":
+        return run_serve(args)
     return run_ours(args)
 
 

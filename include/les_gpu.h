@@ -199,6 +199,30 @@ int les_gpu_field_mean_noalloc(les_handle *h, int field, double *mean);
 long long les_gpu_launch_count(les_handle *h);
 int les_gpu_last_error(les_handle *h, char *buf, size_t len);
 
+/* ---- batches of resident domains (ensembles, continuous batching) ---------------
+ * A batch holds caller-owned domain handles and a step counter per member.
+ * les_batch_step enqueues one time step (n, nmax) of every member whose n <= nmax,
+ * each on the member's own stream, without host synchronisation, and advances n; the
+ * members' kernels overlap on the GPU.  Members join and leave between steps.  A
+ * member's arithmetic never depends on the others: its result is the same alone and
+ * in any mix.  Calls on one batch are serialised internally.  Cross-stream overlap
+ * is bounded by CUDA_DEVICE_MAX_CONNECTIONS (set it, up to 32, before CUDA starts). */
+typedef struct les_batch les_batch;
+int les_batch_create(les_batch **out);
+int les_batch_destroy(les_batch *b);  /* syncs members; does not destroy their handles */
+/* *ok = 1 if the device's free memory holds one more domain of these dims plus
+ * reserve_bytes (admission by free HBM; les_domain_bytes is the footprint). */
+int les_batch_admit(const les_dims *dims, size_t reserve_bytes, int *ok);
+/* Add a committed handle whose next step is n0 (1 for a fresh domain), run to nmax. */
+int les_batch_add(les_batch *b, les_handle *h, int n0, int nmax, int *slot);
+int les_batch_remove(les_batch *b, int slot);  /* syncs the member first */
+/* One step of every unfinished member; *nlive = members with steps left after it. */
+int les_batch_step(les_batch *b, int *nlive);
+int les_batch_sync(les_batch *b);
+/* *n = the member's next step index (> nmax once finished). */
+int les_batch_slot(les_batch *b, int slot, int *n, int *nmax);
+int les_batch_last_error(les_batch *b, char *buf, size_t len);
+
 /* Profiling: queue `reps` back-to-back launches of one stage on the handle's stream,
  * bracketed by CUDA events, and return the average milliseconds per repetition.
  * The stage really runs (it advances the state).  what: LES_PROF_*. */

@@ -139,7 +139,13 @@ extern "C" size_t les_domain_bytes(int im, int jm, int km) {
   const size_t pi = (size_t)pitch_for(im), nj = (size_t)jm + 4, nk = (size_t)km + 4;
   const size_t field = pi * nj * nk * sizeof(float);
   const size_t part = ((size_t)(im + 63) / 64 + 1) * ((size_t)(jm + 3) / 4 + 1) * (size_t)km * 2 * sizeof(double);
-  return (kNumFields + 3 + 9) * field + pi * nj * nk /*mask bytes*/ + 2 * pi * nj * sizeof(float) + part + 64 * 1024;
+  // deferred-block lists (les_gpu_create): FIX_COUNT lists over the largest grid of those kernels
+  const size_t fused = (size_t)((im + 31) / 32) * ((jm + 1) / 2) * ((km + 3) / 4);
+  const size_t inter = (size_t)((im + 63) / 64) * ((jm + 3) / 4) * km;
+  const size_t march = (size_t)((im + 31) / 32) * ((jm + 7) / 8) * km;
+  const size_t fix = FIX_COUNT * (2 + std::max({fused, inter, march})) * sizeof(int);
+  return (kNumFields + 3 + 9) * field + pi * nj * nk /*mask bytes*/ + 2 * pi * nj * sizeof(float) + part + fix +
+         64 * 1024;
 }
 
 extern "C" int les_gpu_create(const les_dims *dims, const les_params *params, les_handle **out) {

@@ -180,6 +180,15 @@ def load_library(path: str | None = None) -> C.CDLL:
         "les_gpu_launch_count": (C.c_longlong, [vp]),
         "les_gpu_last_error": (C.c_int, [vp, C.c_char_p, C.c_size_t]),
         "les_gpu_profile": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(C.c_double)]),
+        "les_batch_create": (C.c_int, [C.POINTER(vp)]),
+        "les_batch_destroy": (C.c_int, [vp]),
+        "les_batch_admit": (C.c_int, [C.POINTER(LesDims), C.c_size_t, ip_]),
+        "les_batch_add": (C.c_int, [vp, vp, C.c_int, C.c_int, ip_]),
+        "les_batch_remove": (C.c_int, [vp, C.c_int]),
+        "les_batch_step": (C.c_int, [vp, ip_]),
+        "les_batch_sync": (C.c_int, [vp]),
+        "les_batch_slot": (C.c_int, [vp, C.c_int, ip_, ip_]),
+        "les_batch_last_error": (C.c_int, [vp, C.c_char_p, C.c_size_t]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -356,3 +365,68 @@ class Domain:
 
     def launch_count(self) -> int:
         return int(self.lib.les_gpu_launch_count(self._h))
+
+
+class Batch:
+    """Many resident domains stepped together (les_batch_*): each member's step graph on
+    its own stream, members joining and leaving between steps."""
+
+    def __init__(self):
+        self.lib = load_library()
+        self._b = C.c_void_p()
+        rc = self.lib.les_batch_create(C.byref(self._b))
+        if rc:
+            raise RuntimeError(f"les_batch_create failed ({rc})")
+        self.members: dict[int, Domain] = {}
+
+    def _check(self, rc: int, what: str):
+        if rc:
+            buf = C.create_string_buffer(512)
+            self.lib.les_batch_last_error(self._b, buf, 512)
+            raise RuntimeError(f"les_batch_{what} failed ({rc}): {buf.value.decode(errors='replace')}")
+
+    @staticmethod
+    def admit(im: int, jm: int, km: int, reserve_bytes: int = 0) -> bool:
+        """Whether the device's free memory holds one more domain of these dims."""
+        lib = load_library()
+        ok = C.c_int(0)
+        rc = lib.les_batch_admit(C.byref(LesDims(im, jm, km)), reserve_bytes, C.byref(ok))
+        if rc:
+            raise RuntimeError(f"les_batch_admit failed ({rc})")
+        return bool(ok.value)
+
+    def add(self, dom: "Domain", n0: int, nmax: int) -> int:
+        slot = C.c_int(-1)
+        self._check(self.lib.les_batch_add(self._b, dom._h, n0, nmax, C.byref(slot)), "add")
+        self.members[slot.value] = dom
+        return slot.value
+
+    def remove(self, slot: int) -> "Domain":
+        self._check(self.lib.les_batch_remove(self._b, slot), "remove")
+        return self.members.pop(slot)
+
+    def step(self) -> int:
+        """One step of every unfinished member; returns the members with steps left."""
+        live = C.c_int(0)
+        self._check(self.lib.les_batch_step(self._b, C.byref(live)), "step")
+        return live.value
+
+    def sync(self):
+        self._check(self.lib.les_batch_sync(self._b), "sync")
+
+    def progress(self, slot: int) -> tuple[int, int]:
+        """(next step index, nmax) of a member; finished once next > nmax."""
+        n, nmax = C.c_int(0), C.c_int(0)
+        self._check(self.lib.les_batch_slot(self._b, slot, C.byref(n), C.byref(nmax)), "slot")
+        return n.value, nmax.value
+
+    def close(self):
+        if self._b:
+            self.lib.les_batch_destroy(self._b)
+            self._b = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

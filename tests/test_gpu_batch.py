@@ -1,0 +1,101 @@
+"""Batches of resident domains (les_batch_*) and the serving loop on the GPU.
+
+The contract of batching: a domain's result does not depend on the company it is
+stepped in -- alone, in a batch, joined mid-way by others -- bit for bit.
+"""
+import numpy as np
+import pytest
+
+import lesgpu
+import serve
+from helpers import make_gpu, make_ref, rel_err, scenario
+
+pytestmark = pytest.mark.gpu
+
+
+def _alone(sc, params, nsteps):
+    d = make_gpu(sc, params)
+    for n in range(1, nsteps + 1):
+        d.step(n, nsteps)
+    d.sync()
+    return d
+
+
+def _same(a, b, what):
+    for fid in lesgpu.STATE_FIELDS:
+        x, y = a.download(fid), b.download(fid)
+        assert np.array_equal(x.view(np.uint32), y.view(np.uint32)), (what, lesgpu.FIELD_NAMES[fid])
+
+
+def test_batch_member_same_alone_and_in_mix(built_lib):
+    params = lesgpu.Params(nmaxp=8)
+    sa = scenario(48, 30, 14, seed=81, direction_deg=30.0, u_ref=4.0)
+    sb = scenario(64, 40, 12, seed=82, direction_deg=200.0, u_ref=8.0)
+    sc_ = scenario(37, 18, 11, seed=83, direction_deg=95.0)  # odd jm: the per-subroutine SOR path
+    ref_a = _alone(sa, params, 6)
+    ref_c = _alone(sc_, params, 4)
+    b = lesgpu.Batch()
+    a, bb, c = make_gpu(sa, params), make_gpu(sb, params), make_gpu(sc_, params)
+    sa_slot = b.add(a, 1, 6)
+    b.add(bb, 1, 9)
+    steps = 0
+    while True:
+        if steps == 2:
+            sc_slot = b.add(c, 1, 4)  # joins mid-way
+        live = b.step()
+        steps += 1
+        if live == 0 and steps > 2:
+            break
+    b.sync()
+    assert b.progress(sa_slot) == (7, 6) and b.progress(sc_slot) == (5, 4)
+    _same(a, ref_a, "a")
+    _same(c, ref_c, "c")
+    b.remove(sa_slot)
+    b.close()
+
+
+def test_batch_members_vs_fp64_oracle(built_lib):
+    """Ensemble members with their own seed, inflow direction and speed: each within
+    the 1e-4 contract of the FP64 oracle after 8 steps."""
+    params = lesgpu.Params()
+    scs = [scenario(40, 24, 16, seed=91 + q, direction_deg=d, u_ref=s)
+           for q, (d, s) in enumerate(((20.0, 3.0), (135.0, 9.0), (290.0, 6.0)))]
+    b = lesgpu.Batch()
+    doms = [make_gpu(sc, params) for sc in scs]
+    for d in doms:
+        b.add(d, 1, 8)
+    while b.step() > 0:
+        pass
+    b.sync()
+    for sc, d in zip(scs, doms):
+        orc = make_ref(8, sc, params, sqrt_half=0, red64=1)
+        for n in range(1, 9):
+            orc.step(n, 8)
+        for fid in (lesgpu.U, lesgpu.V, lesgpu.W, lesgpu.P):
+            g = d.download(fid, (1, 1, 1), (sc.im, sc.jm, sc.km)).astype(np.float64)
+            o = orc.get(fid, (1, 1, 1), (sc.im, sc.jm, sc.km))
+            assert rel_err(g, o) <= 1e-4, (sc.seed, lesgpu.FIELD_NAMES[fid])
+    b.close()
+
+
+def test_serving_small_stream_matches_alone(built_lib):
+    """A short request stream through the server: every request completes, and a
+    request's final state equals the same scenario stepped alone."""
+    reqs = [serve.Request(q, 0.03 * q, im, jm, km, 100 + q, 37.0 * q, 3.0 + q, 0.3, steps)
+            for q, (im, jm, km, steps) in enumerate(((32, 24, 10, 5), (48, 32, 12, 7), (40, 20, 9, 3),
+                                                     (32, 32, 16, 6), (24, 16, 8, 4)))]
+    be = serve.GpuBackend(reserve_bytes=1 << 30)
+    kept = {}
+
+    def on_done(r, dom):
+        kept[r.rid] = {fid: dom.download(fid) for fid in (lesgpu.U, lesgpu.V, lesgpu.W, lesgpu.P)}
+
+    stats = serve.Server(be, setup_workers=2, on_done=on_done).run(reqs)
+    assert stats["completed"] == len(reqs) and stats["rejected"] == 0
+    assert stats["latency_s"]["p99"] is not None
+    for r in (reqs[1], reqs[3]):
+        alone = _alone(be.scenario(r), lesgpu.Params(), r.steps)
+        for fid, x in kept[r.rid].items():
+            y = alone.download(fid)
+            assert np.array_equal(x.view(np.uint32), y.view(np.uint32)), (r.rid, lesgpu.FIELD_NAMES[fid])
+    be.batch.close()
