@@ -190,18 +190,3 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
   const float bb = s - a;
   e = (a - (s - bb)) + (b - bb);
 }
-// Sum of one FP32 term per lane, returned in FP64 on lane 0.  The warp tree carries an
-// unevaluated pair (hi, lo): hi adds by TwoSum, lo gathers the rounding errors, so the
-// FP64 pipe (slow on this part) is touched once per warp, not once per term.  The
-// error stays near 2^-47 of the sum of magnitudes; the order is fixed (deterministic).
-__device__ __forceinline__ double warp_sum_pair(float x) {
-  float hi = x, lo = 0.f;
-  for (int o = 16; o > 0; o >>= 1) {
-    const float h2 = __shfl_down_sync(0xffffffffu, hi, o), l2 = __shfl_down_sync(0xffffffffu, lo, o);
-    float s, e;
-    two_sum(hi, h2, s, e);
-    hi = s;
-    lo = (lo + l2) + e;
-  }
-  return (double)hi + (double)lo;
-}

@@ -241,46 +241,74 @@ __device__ __forceinline__ float rhs_cell(const LesDom &d, int i, int j, int k, 
          dvs<P2, ZF>(__ldg(g + c) - __ldg(g + c - d.pi), dy1[j], ry, bd) +
          dvz<ZF>(__ldg(h + c) - __ldg(h + c - d.np), dzn[k], rz, bd) + dvz<ZF>(r, d.dt, d.rdt, bd);
 }
-// Block sum of one FP32 term per thread (BX x BY threads) into part[slot]: warp pairs
-// (warp_sum_pair), then the warps in FP64 in order.
-__device__ __forceinline__ void block_part(const LesDom &d, float term, int slot) {
+// Compensated running sum of FP32 terms: hi by TwoSum, lo gathers the rounding errors.
+struct PairSum {
+  float hi = 0.f, lo = 0.f;
+  __device__ __forceinline__ void add(float t) {
+    float s, e;
+    two_sum(hi, t, s, e);
+    hi = s;
+    lo += e;
+  }
+};
+// Block sum of each thread's pair (BX x BY threads) into part[slot]: warp trees of
+// pairs, then the warps in FP64 in order.
+__device__ __forceinline__ void block_part(const LesDom &d, PairSum p, int slot) {
   __shared__ double sh[BX * BY / 32];
   const int tid = threadIdx.y * BX + threadIdx.x;
-  const double x = warp_sum_pair(term);
-  if ((tid & 31) == 0) sh[tid >> 5] = x;
+  float hi = p.hi, lo = p.lo;
+  for (int o = 16; o > 0; o >>= 1) {
+    const float h2 = __shfl_down_sync(0xffffffffu, hi, o), l2 = __shfl_down_sync(0xffffffffu, lo, o);
+    float s, e;
+    two_sum(hi, h2, s, e);
+    hi = s;
+    lo = (lo + l2) + e;
+  }
+  if ((tid & 31) == 0) sh[tid >> 5] = (double)hi + (double)lo;
   __syncthreads();
   if (tid == 0) {
     double s = 0.0;
     for (int q = 0; q < BX * BY / 32; ++q) s += sh[q];
     d.part[slot] = s;
   }
+  __syncthreads();  // sh is reused when a fixup CTA loops over several blocks
 }
 
-// rhs of the block (bx, by, bz) of grid g, plus its partial of
-// sum(dx1*dy1*dzn*rhs) (press.f95:63-72).  dst: the rhs array (rhs = d.rhs) or the
-// SOR's internal rhs buffer, which also takes periodic ghost copies of rows 1, 2,
-// jm-1, jm in rows jm+1, jm+2, -1, 0.  ZF as in velnw_block.
+// k planes per block of the reduction kernels (one partial per BX x BY x RKC cells)
+constexpr int RKC = 16;
+inline dim3 reduce_grid(const LesDom &d) { return dim3((d.im + BX - 1) / BX, (d.jm + BY - 1) / BY, (d.km + RKC - 1) / RKC); }
+
+// rhs of the cells of block (bx, by, bz) -- columns (i, j), planes bz*RKC+1 .. -- plus
+// its partial of sum(dx1*dy1*dzn*rhs) (press.f95:63-72).  dst: the rhs array (rhs =
+// d.rhs) or the SOR's internal rhs buffer, which also takes periodic ghost copies of
+// rows 1, 2, jm-1, jm in rows jm+1, jm+2, -1, 0.  ZF: reciprocal-corrected divisions;
+// a block that met a dividend outside their range is recomputed whole by the fixup
+// (rhs only reads u, v, w, f, g, h, so recomputing overwrites with the same cells).
 template <bool P2, bool ZF>
 __device__ __forceinline__ void rhs_block(const LesDom &d, float *dst, int ghost, int bx, int by, int bz, uint3 g) {
-  const int i0 = bx * BX + threadIdx.x + 1, j0 = by * BY + threadIdx.y + 1, k = bz + 1;
+  const int i0 = bx * BX + threadIdx.x + 1, j0 = by * BY + threadIdx.y + 1;
   const bool in = (i0 <= d.im && j0 <= d.jm);
   const int i = min(i0, d.im), j = min(j0, d.jm);  // past the edge: the edge cell again, not stored
-  const int c = lix(d, i, j, k);
+  const int ka = bz * RKC + 1, kb = min(ka + RKC - 1, d.km);
+  const float axy = d.gr.dx1[i] * d.gr.dy1[j];
   unsigned bd = 0;
-  const float rr = rhs_cell<P2, ZF>(d, i, j, k, c, bd);
-  if (ZF && defer_block(bd, d.fix[FIX_RHS])) return;
-  float term = 0.f;
-  if (in) {
-    dst[c] = rr;
-    if (ghost) {
-      if (j == 1) dst[lix(d, i, d.jm + 1, k)] = rr;
-      if (j == 2) dst[lix(d, i, d.jm + 2, k)] = rr;
-      if (j == d.jm - 1) dst[lix(d, i, -1, k)] = rr;
-      if (j == d.jm) dst[lix(d, i, 0, k)] = rr;
+  PairSum acc;
+  for (int k = ka; k <= kb; ++k) {
+    const int c = lix(d, i, j, k);
+    const float rr = rhs_cell<P2, ZF>(d, i, j, k, c, bd);
+    if (in) {
+      dst[c] = rr;
+      if (ghost) {
+        if (j == 1) dst[lix(d, i, d.jm + 1, k)] = rr;
+        if (j == 2) dst[lix(d, i, d.jm + 2, k)] = rr;
+        if (j == d.jm - 1) dst[lix(d, i, -1, k)] = rr;
+        if (j == d.jm) dst[lix(d, i, 0, k)] = rr;
+      }
+      acc.add(axy * d.gr.dzn[k] * rr);
     }
-    term = d.gr.dx1[i] * d.gr.dy1[j] * d.gr.dzn[k] * rr;
   }
-  block_part(d, term, (int)((bz * g.y + by) * g.x + bx));
+  if (ZF && defer_block(bd, d.fix[FIX_RHS])) return;
+  block_part(d, acc, (int)((bz * g.y + by) * g.x + bx));
 }
 template <bool P2, bool ZF>
 __global__ void __launch_bounds__(BX *BY) k_rhs(LesDom d, float *dst, int ghost) {
@@ -290,14 +318,17 @@ template <bool P2>
 __global__ void __launch_bounds__(BX *BY) k_rhs_fix(LesDom d, float *dst, int ghost, uint3 g) {
   for_deferred(d.fix[FIX_RHS], g, [&](int bx, int by, int bz) { rhs_block<P2, false>(d, dst, ghost, bx, by, bz, g); });
 }
-// pav partials: sum(p*dx1*dy1*dzn) (press.f95:124-133)
+// pav partials: sum(p*dx1*dy1*dzn) (press.f95:124-133), one per block of RKC planes
 __global__ void __launch_bounds__(BX *BY) k_pav_part(LesDom d) {
   const int i = blockIdx.x * BX + threadIdx.x + 1;
   const int j = blockIdx.y * BY + threadIdx.y + 1;
-  const int k = blockIdx.z + 1;
-  float term = 0.f;
-  if (i <= d.im && j <= d.jm) term = __ldg(d.p + lix(d, i, j, k)) * d.gr.dx1[i] * d.gr.dy1[j] * d.gr.dzn[k];
-  block_part(d, term, (int)((blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x));
+  const int ka = blockIdx.z * RKC + 1, kb = min(ka + RKC - 1, d.km);
+  PairSum acc;
+  if (i <= d.im && j <= d.jm) {
+    const float dx = d.gr.dx1[i], dy = d.gr.dy1[j];
+    for (int k = ka; k <= kb; ++k) acc.add(__ldg(d.p + lix(d, i, j, k)) * dx * dy * d.gr.dzn[k]);
+  }
+  block_part(d, acc, (int)((blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x));
 }
 // mean = (float)(sum of partials / area), summed in a fixed order: FIN_BLOCKS chunks,
 // each a strided FP64 sum and a fixed tree, then the chunks in order by the last block
@@ -469,7 +500,7 @@ void les_launch_velnw(const LesDom &d, LesCtx ctx) {
 
 // rhs into dst, its fixup, and the mean
 static void launch_rhs(const LesDom &d, float *dst, int ghost, LesCtx ctx) {
-  const dim3 g = interior_grid(d, d.km), b(BX, BY);
+  const dim3 g = reduce_grid(d), b(BX, BY);
   LAUNCH(ctx, LES_PZ_SWITCH(d, k_rhs, <<<g, b, 0, ctx.s>>>(d, dst, ghost)));
   if (d.zfast) {
     if (d.xy_pow2) LAUNCH(ctx, (k_rhs_fix<true><<<fix_grid(d, g), b, 0, ctx.s>>>(d, dst, ghost, u3(g))));
@@ -554,13 +585,15 @@ int les_sor_simple_parts(const LesDom &d) {
 }
 
 void les_launch_interior_mean(const LesDom &d, LesCtx ctx) {
-  LAUNCH(ctx, k_pav_part<<<interior_grid(d, d.km), dim3(BX, BY), 0, ctx.s>>>(d));
-  LAUNCH(ctx, k_finish_mean<<<FIN_BLOCKS, FIN_THREADS, 0, ctx.s>>>(d, les_interior_blocks(d), SC_PAV));
+  const dim3 g = reduce_grid(d);
+  LAUNCH(ctx, k_pav_part<<<g, dim3(BX, BY), 0, ctx.s>>>(d));
+  LAUNCH(ctx, k_finish_mean<<<FIN_BLOCKS, FIN_THREADS, 0, ctx.s>>>(d, (int)(g.x * g.y * g.z), SC_PAV));
 }
 
 void les_launch_pav_adjust(const LesDom &d, LesCtx ctx) {
-  const int nb = les_interior_blocks(d);
-  LAUNCH(ctx, k_pav_part<<<interior_grid(d, d.km), dim3(BX, BY), 0, ctx.s>>>(d));
+  const dim3 gr = reduce_grid(d);
+  const int nb = (int)(gr.x * gr.y * gr.z);
+  LAUNCH(ctx, k_pav_part<<<gr, dim3(BX, BY), 0, ctx.s>>>(d));
   LAUNCH(ctx, k_finish_mean<<<FIN_BLOCKS, FIN_THREADS, 0, ctx.s>>>(d, nb, SC_PAV));
   LAUNCH(ctx, k_sub_mean<<<interior_grid(d, d.km), dim3(BX, BY), 0, ctx.s>>>(d, d.p, SC_PAV));
   les_launch_boundp1(d, ctx, 0);
