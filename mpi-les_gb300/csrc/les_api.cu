@@ -212,7 +212,7 @@ extern "C" int les_gpu_create(const les_dims *dims, const les_params *params, le
   h->mask_h.assign(h->nfloat, 0);
   // partial-sum buffer: the largest per-block count of any reduction kernel
   h->npart = (size_t)std::max<long long>(
-      {(long long)((im + 63) / 64) * ((jm + 3) / 4) * km * 2 + 64, (long long)les_step_parts_needed(im, jm, km)});
+      {(long long)((im + 63) / 64) * ((jm + 3) / 4) * km * 2 + 64, (long long)les_step_parts_needed(im, jm, km, h->sms)});
   // deferred-block lists: [count, ticket, ids...] for the largest grid of those kernels
   {
     const long long fused = (long long)((im + 31) / 32) * ((jm + 1) / 2) * ((km + 3) / 4);

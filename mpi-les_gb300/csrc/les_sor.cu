@@ -30,12 +30,20 @@
 // ghost rows (j = -1, 0, jm+1, jm+2), so a tile plane is a plain rectangle that one
 // tensor TMA copy can bring in; the last iteration writes p.
 //
+// k chunks: when the tiles alone would leave SMs idle (small domains), grid z splits
+// the march into chunks of planes [ka, kb] (the KC kernel variants).  A chunk starts
+// one plane early, at ka-1, relaxing its red cells as a ring plane (from the old black
+// values around it, exactly as the chunk below does) so that its black cells of plane
+// ka have their red neighbours; ring planes are neither stored nor counted in the
+// residual.
+//
 // Residual: each thread accumulates reltmp^2 of its owned cells in FP32 with Kahan
 // compensation, CTAs reduce to FP64 partials, and the last CTA to finish sums them in
 // a fixed order (no spin waits) and applies the convergence test of press.f95:119.
 #include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdlib>
 
 #include "les_common.cuh"
@@ -168,7 +176,7 @@ __device__ __forceinline__ void finish_residual(const LesDom &d, const SorArgs &
   for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
   if (c4 == 0) warp[r] = (double)x;
   __syncthreads();
-  const int cta = blockIdx.y * gridDim.x + blockIdx.x;
+  const int cta = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
   if (r == 0 && c4 == 0) {
     double t = 0.0;
     for (int q = 0; q < NY; ++q) t += warp[q];
@@ -206,7 +214,7 @@ struct IC {
 // Register kernel: each thread loads its own float4 columns straight into registers,
 // prefetched three march steps ahead.  Reads j ring rows by wrapping, so it runs on p
 // itself (the first iteration) and on any cn1 (uniform, stored or separable).
-template <int NY, int CN1MODE>
+template <int NY, int CN1MODE, bool KC>
 __global__ void __launch_bounds__(NX *NY, 1) k_sor_reg(LesDom d, SorArgs a) {
   __shared__ float4 sOld[2][NY][NX];
   __shared__ float4 sRed[2][NY][NX];
@@ -219,6 +227,11 @@ __global__ void __launch_bounds__(NX *NY, 1) k_sor_reg(LesDom d, SorArgs a) {
   const int c4 = L.c4, r = L.r, ib = L.ib, jw = L.jw;
   const int im = d.im, jm = d.jm, km = d.km;
   const bool col_load = (ib <= im + 1);
+  // this CTA's k chunk [ka, kb], marched from ka-1 (a red ring plane) to kb+1
+  const int ka = KC ? 1 + (int)blockIdx.z * a.kchunk : 1;
+  const int kb = KC ? min(km, ka + a.kchunk - 1) : km;
+  const int s_begin = KC ? max(1, ka - 1) : 1;
+  const int s_end = KC ? min(km + 1, kb + 1) : km + 1;
 
   for (int q = r * NX + c4; q <= km; q += NX * NY) {
     if (q >= 1) {
@@ -264,12 +277,30 @@ __global__ void __launch_bounds__(NX *NY, 1) k_sor_reg(LesDom d, SorArgs a) {
   // loads issued for planes s+4 (p) and s+3 (rhs) land in the slots just freed and are
   // first used three steps later, so their latency overlaps three steps of work.
   float4 P[6], R[6];
-  P[0] = ldp(0); P[1] = ldp(1); P[2] = ldp(2); P[3] = ldp(3); P[4] = ldp(4); P[5] = zero4;
-  R[0] = zero4; R[1] = ldr(1); R[2] = ldr(2); R[3] = ldr(3); R[4] = zero4; R[5] = zero4;
+  if (!KC) {
+    P[0] = ldp(0); P[1] = ldp(1); P[2] = ldp(2); P[3] = ldp(3); P[4] = ldp(4); P[5] = zero4;
+    R[0] = zero4; R[1] = ldr(1); R[2] = ldr(2); R[3] = ldr(3); R[4] = zero4; R[5] = zero4;
+  } else {
+    // planes s_begin-1 .. s_begin+3 of p and s_begin .. s_begin+2 of rhs, in slot plane % 6
+#pragma unroll
+    for (int t = 0; t < 6; ++t) P[t] = R[t] = zero4;
+#pragma unroll
+    for (int q = 0; q < 5; ++q) {
+      const int m = s_begin - 1 + q, slot = m % 6;
+#pragma unroll
+      for (int t = 0; t < 6; ++t)
+        if (t == slot) {
+          P[t] = ldp(m);
+          if (q >= 1 && q <= 3) R[t] = ldr(m);
+        }
+    }
+  }
   float acc = 0.f, comp = 0.f;
 
   auto step = [&](auto UC, int s) {
     constexpr int U = decltype(UC)::value;
+    if (KC && s < s_begin) return;  // before this chunk's start (the unrolled march is aligned to 6)
+    const bool inr = !KC || (s >= ka && s <= kb);  // red of an owned plane (not a ring plane)
     constexpr int S0 = (1 + U) % 6, SM1 = (S0 + 5) % 6, SM2 = (S0 + 4) % 6, SP1 = (S0 + 1) % 6;
     constexpr int RP3 = (S0 + 3) % 6;
     constexpr int B = (1 + U) & 1, BB = U & 1;  // shared-memory parities of planes s, s-1
@@ -289,7 +320,7 @@ __global__ void __launch_bounds__(NX *NY, 1) k_sor_reg(LesDom d, SorArgs a) {
       const float c4l = sC4l[s], c4s = sC4s[s];
       if (CN1MODE == 0) {
         part += relax_pair(q, P[S0], pl, pr, pn, pso, P[SP1], P[SM1], R[S0], rhsav, omega, sCk[s], c2l, c2s,
-                           c3l, c3s, c4l, c4s, L.west0, L.east_e, L.owned, L.ival);
+                           c3l, c3s, c4l, c4s, L.west0, L.east_e, L.owned && inr, L.ival);
       } else {
         const float4 cur = P[S0];
 #pragma unroll
@@ -303,13 +334,13 @@ __global__ void __launch_bounds__(NX *NY, 1) k_sor_reg(LesDom d, SorArgs a) {
                                  f4get(pso, e), c4l, f4get(P[SP1], e), c4s, f4get(P[SM1], e),
                                  f4get(R[S0], e) - rhsav, pc);
           f4set(P[S0], e, pc + rt);
-          if (L.owned) part += rt * rt;
+          if (L.owned && inr) part += rt * rt;
         }
       }
     }
     sRed[B][r][c4] = P[S0];
     // ---- black cells of plane s-1 on the tile
-    if (s >= 2 && L.owned) {
+    if ((KC ? (s - 1 >= ka && s - 1 <= kb) : (s >= 2)) && L.owned) {
       const int k = s - 1;
       const float4 pn = sRed[BB][r + 1][c4], pso = sRed[BB][r - 1][c4];
       const float pl = bpl, pr = bpr;
@@ -345,17 +376,17 @@ __global__ void __launch_bounds__(NX *NY, 1) k_sor_reg(LesDom d, SorArgs a) {
     R[RP3] = ldr(s + 3);
   };
 
-  for (int s0 = 1; s0 <= km + 1; s0 += 6) {
+  for (int s0 = KC ? s_begin - (s_begin - 1) % 6 : 1; s0 <= s_end; s0 += 6) {
     step(IC<0>{}, s0);
-    if (s0 + 1 > km + 1) break;
+    if (s0 + 1 > s_end) break;
     step(IC<1>{}, s0 + 1);
-    if (s0 + 2 > km + 1) break;
+    if (s0 + 2 > s_end) break;
     step(IC<2>{}, s0 + 2);
-    if (s0 + 3 > km + 1) break;
+    if (s0 + 3 > s_end) break;
     step(IC<3>{}, s0 + 3);
-    if (s0 + 4 > km + 1) break;
+    if (s0 + 4 > s_end) break;
     step(IC<4>{}, s0 + 4);
-    if (s0 + 5 > km + 1) break;
+    if (s0 + 5 > s_end) break;
     step(IC<5>{}, s0 + 5);
   }
   finish_residual<NY>(d, a, acc, sWarp, &sLast);
@@ -413,7 +444,7 @@ struct TmaSmem {
   int last, abort_;
 };
 
-template <int NY, int D>
+template <int NY, int D, bool KC>
 __global__ void __launch_bounds__(NX *NY, 1)
     k_sor_tma(LesDom d, SorArgs a, const __grid_constant__ CUtensorMap tmP, const __grid_constant__ CUtensorMap tmR) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -436,8 +467,16 @@ __global__ void __launch_bounds__(NX *NY, 1)
   const int tx = blockIdx.x * TI;   // padded column of i0 - 4
   const int ty = blockIdx.y * a.tj; // padded row of j0 - 2
   const uint32_t stage_bytes = 2u * NY * NX * 16u;
-  auto issue = [&](int m) {  // plane m (1..km) into stage (m-1) % D
-    const int q = (m - 1) % D;
+  // this CTA's k chunk [ka, kb], marched from ka-1 (a red ring plane) to kb+1; it
+  // loads planes mfirst .. mlast, plane m into stage (m - mfirst) % D
+  const int ka = KC ? 1 + (int)blockIdx.z * a.kchunk : 1;
+  const int kb = KC ? min(km, ka + a.kchunk - 1) : km;
+  const int s_begin = KC ? max(1, ka - 1) : 1;
+  const int s_end = KC ? min(km + 1, kb + 1) : km + 1;
+  const int mfirst = KC ? max(1, s_begin - 1) : 1;
+  const int mlast = KC ? min(km, kb + 2) : km;
+  auto issue = [&](int m) {  // plane m (mfirst..mlast) into stage (m - mfirst) % D
+    const int q = (m - mfirst) % D;
     mbar_expect_tx(&S.bar[q], stage_bytes);
     tma_load_3d(&S.p[q][0][0], &tmP, tx, ty, m + LES_KOFF, &S.bar[q]);
     tma_load_3d(&S.rhs[q][0][0], &tmR, tx, ty, m + LES_KOFF, &S.bar[q]);
@@ -457,31 +496,36 @@ __global__ void __launch_bounds__(NX *NY, 1)
   }
   __syncthreads();
   if (producer)
-    for (int m = 1; m <= D && m <= km; ++m) issue(m);
+    for (int m = mfirst; m < mfirst + D && m <= mlast; ++m) issue(m);
 
   int failed_at = 0;
   auto wait_plane = [&](int m) {
-    if (!mbar_wait(&S.bar[(m - 1) % D], (uint32_t)(((m - 1) / D) & 1))) {
+    if (!mbar_wait(&S.bar[(m - mfirst) % D], (uint32_t)(((m - mfirst) / D) & 1))) {
       S.abort_ = 1;
       d.ctl[CT_ERROR] = 1;
       if (!failed_at) failed_at = m;
     }
   };
 
-  wait_plane(1);
   const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
-  float4 Pm2 = zero4, Pm1 = zero4, P0 = S.p[0][r][c4], Rm1 = zero4;
+  float4 Pm2 = zero4, Pm1 = zero4, P0 = zero4, Rm1 = zero4;
+  if (KC && s_begin > 1) {
+    wait_plane(s_begin - 1);
+    Pm1 = S.p[(s_begin - 1 - mfirst) % D][r][c4];
+  }
+  wait_plane(s_begin);
+  P0 = S.p[(s_begin - mfirst) % D][r][c4];
   float acc = 0.f, comp = 0.f;
 
-  for (int s = 1; s <= km + 1; ++s) {
+  for (int s = s_begin; s <= s_end; ++s) {
     __syncthreads();
     if (S.abort_) continue;
-    // the stage of plane s-1 is free: every thread has left step s-1
-    if (producer && s >= 2 && s - 1 + D <= km) issue(s - 1 + D);
+    // the stage of plane s-1 is free: every thread has left step s-1 (or the prologue)
+    if (producer && s - 1 >= mfirst && s - 1 + D <= mlast) issue(s - 1 + D);
     float4 P1 = P0, R0 = zero4;
-    if (s + 1 <= km) {
+    if (s + 1 <= mlast) {
       wait_plane(s + 1);
-      P1 = S.p[s % D][r][c4];
+      P1 = S.p[(s + 1 - mfirst) % D][r][c4];
     }
     float part = 0.f;
     const int B = s & 1, BB = (s - 1) & 1;
@@ -492,7 +536,7 @@ __global__ void __launch_bounds__(NX *NY, 1)
     const float bpl = __shfl_up_sync(0xffffffffu, Pm1.w, 1);
     const float bpr = __shfl_down_sync(0xffffffffu, Pm1.x, 1);
     if (s <= km && L.row_red) {
-      const int st = (s - 1) % D;
+      const int st = (s - mfirst) % D;
       R0 = S.rhs[st][r][c4];
       const float4 pn = S.p[st][r + 1][c4], pso = S.p[st][r - 1][c4];
       const float pl = rpl, pr = rpr;
@@ -500,10 +544,10 @@ __global__ void __launch_bounds__(NX *NY, 1)
       const float4 up = (s == km) ? P0 : P1;
       const float4 dn = (s == 1) ? P0 : Pm1;
       part += relax_pair(q, P0, pl, pr, pn, pso, up, dn, R0, rhsav, omega, S.ck[s], c2l, c2s, c3l, c3s,
-                         S.c4l[s], S.c4s[s], L.west0, L.east_e, L.owned, L.ival);
+                         S.c4l[s], S.c4s[s], L.west0, L.east_e, L.owned && (!KC || (s >= ka && s <= kb)), L.ival);
     }
     S.red[B][r][c4] = P0;
-    if (s >= 2 && L.owned) {
+    if ((KC ? (s - 1 >= ka && s - 1 <= kb) : (s >= 2)) && L.owned) {
       const int k = s - 1;
       const float4 pn = S.red[BB][r + 1][c4], pso = S.red[BB][r - 1][c4];
       const float pl = bpl, pr = bpr;
@@ -526,8 +570,8 @@ __global__ void __launch_bounds__(NX *NY, 1)
   }
   // after a failed wait, wait (bounded) for the copies already issued before leaving
   if (failed_at) {
-    for (int m = failed_at; m <= km && m < failed_at + D; ++m)
-      (void)mbar_wait(&S.bar[(m - 1) % D], (uint32_t)(((m - 1) / D) & 1));
+    for (int m = failed_at; m <= mlast && m < failed_at + D; ++m)
+      (void)mbar_wait(&S.bar[(m - mfirst) % D], (uint32_t)(((m - mfirst) / D) & 1));
   }
   finish_residual<NY>(d, a, acc, S.warp, &S.last);
 }
@@ -548,21 +592,31 @@ __global__ void k_sor_copyout(LesDom d, int nmaxp) {
   }
 }
 
+template <int NY, bool KC>
+void launch_reg_kc(const LesDom &d, const SorArgs &a, int cn1mode, cudaStream_t s) {
+  const dim3 grid((d.im + TI - 1) / TI, (d.jm + a.tj - 1) / a.tj, KC ? a.nchunk : 1);
+  const dim3 block(NX, NY);
+  if (cn1mode == 1) k_sor_reg<NY, 1, KC><<<grid, block, 0, s>>>(d, a);
+  else if (cn1mode == 2) k_sor_reg<NY, 2, KC><<<grid, block, 0, s>>>(d, a);
+  else k_sor_reg<NY, 0, KC><<<grid, block, 0, s>>>(d, a);
+}
 template <int NY>
 void launch_reg(const LesDom &d, const SorArgs &a, int cn1mode, cudaStream_t s) {
-  const dim3 grid((d.im + TI - 1) / TI, (d.jm + a.tj - 1) / a.tj);
-  const dim3 block(NX, NY);
-  if (cn1mode == 1) k_sor_reg<NY, 1><<<grid, block, 0, s>>>(d, a);
-  else if (cn1mode == 2) k_sor_reg<NY, 2><<<grid, block, 0, s>>>(d, a);
-  else k_sor_reg<NY, 0><<<grid, block, 0, s>>>(d, a);
+  if (a.nchunk > 1) launch_reg_kc<NY, true>(d, a, cn1mode, s);
+  else launch_reg_kc<NY, false>(d, a, cn1mode, s);
 }
 
+template <int NY, int D, bool KC>
+void launch_tma_kc(const LesDom &d, const SorArgs &a, const CUtensorMap &tp, const CUtensorMap &tr, cudaStream_t s) {
+  const dim3 grid((d.im + TI - 1) / TI, (d.jm + a.tj - 1) / a.tj, KC ? a.nchunk : 1);
+  const size_t bytes = sizeof(TmaSmem<NY, D>);
+  cudaFuncSetAttribute(k_sor_tma<NY, D, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  k_sor_tma<NY, D, KC><<<grid, dim3(NX, NY), bytes, s>>>(d, a, tp, tr);
+}
 template <int NY, int D>
 void launch_tma(const LesDom &d, const SorArgs &a, const CUtensorMap &tp, const CUtensorMap &tr, cudaStream_t s) {
-  const dim3 grid((d.im + TI - 1) / TI, (d.jm + a.tj - 1) / a.tj);
-  const size_t bytes = sizeof(TmaSmem<NY, D>);
-  cudaFuncSetAttribute(k_sor_tma<NY, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-  k_sor_tma<NY, D><<<grid, dim3(NX, NY), bytes, s>>>(d, a, tp, tr);
+  if (a.nchunk > 1) launch_tma_kc<NY, D, true>(d, a, tp, tr, s);
+  else launch_tma_kc<NY, D, false>(d, a, tp, tr, s);
 }
 
 }  // namespace
@@ -585,6 +639,17 @@ int les_sor_pick_ny(int im, int jm, int sms) {
     if (cost < best_cost - 1e-9) { best_cost = cost; best = ny; }
   }
   return best;
+}
+
+int les_sor_pick_kchunk(int tiles, int km, int sms) {
+  if (const char *e = getenv("LES_SOR_KCHUNK")) {  // A/B measurements
+    const int v = atoi(e);
+    if (v > 0) return v;
+  }
+  if (tiles <= 0 || 2 * tiles >= sms) return km;
+  int nch = (sms + tiles - 1) / tiles;
+  nch = std::max(1, std::min(nch, km / 8));
+  return (km + nch - 1) / nch;
 }
 
 int les_sor_make_maps(const LesDom &d, int ny, LesSorMaps *maps) {

@@ -17,6 +17,8 @@ struct SorArgs {
   double *part;          // per-CTA residual partials (>= ntiles)
   unsigned int *counter; // CTA completion ticket, zero between launches
   int ghost;             // 1: also write pdst's periodic ghost rows (internal buffers)
+  int kchunk;            // k planes per CTA (grid z = nchunk chunks); >= km: one chunk
+  int nchunk;            // chunks (grid z)
 };
 
 // Tensor maps of the internal buffers (sorA, sorB, sorR) for one tile height.
@@ -28,6 +30,9 @@ struct LesSorMaps {
 
 int les_sor_fused_tiles(int im, int jm, int ny);
 int les_sor_pick_ny(int im, int jm, int sms);
+// Planes per k chunk: one chunk when the tiles fill the SMs, else enough chunks to
+// fill them (each at least 8 planes: a chunk recomputes one red plane below it).
+int les_sor_pick_kchunk(int tiles, int km, int sms);
 int les_sor_make_maps(const LesDom &d, int ny, LesSorMaps *maps);
 // One SOR iteration: the TMA kernel when the source is an internal buffer with valid
 // maps and cn1 is uniform, the register kernel otherwise.

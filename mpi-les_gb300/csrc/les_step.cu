@@ -14,12 +14,13 @@
 #include "les_sor.cuh"
 #include "les_step.cuh"
 
-int les_step_parts_needed(int im, int jm, int km) {
-  (void)km;
+int les_step_parts_needed(int im, int jm, int km, int sms) {
   int worst = 0;
   for (int ny = 16; ny <= 32; ny += 4) {
     const int t = les_sor_fused_tiles(im, jm, ny);
-    worst = t > worst ? t : worst;
+    const int kc = les_sor_pick_kchunk(t, km, sms > 0 ? sms : 152);
+    const int parts = t * ((km + kc - 1) / kc);
+    worst = parts > worst ? parts : worst;
   }
   return worst + 64;
 }
@@ -51,7 +52,9 @@ int les_step_pick_ny(const LesDom &d) {
 static void enqueue_sor_fused(const LesDom &d, const les_params &prm, int ny, const LesSorMaps *maps, LesCtx ctx) {
   les_launch_sor_begin(d, ctx);
   const int nit = prm.nmaxp;
-  const int ntiles = les_sor_fused_tiles(d.im, d.jm, ny);
+  const int tiles = les_sor_fused_tiles(d.im, d.jm, ny);
+  const int kchunk = les_sor_pick_kchunk(tiles, d.km, d.sms > 0 ? d.sms : 152);
+  const int nchunk = (d.km + kchunk - 1) / kchunk;
   for (int l = 1; l <= nit; ++l) {
     SorArgs a;
     a.psrc = (l == 1) ? d.p : (((l - 1) & 1) ? d.sorB : d.sorA);
@@ -60,7 +63,9 @@ static void enqueue_sor_fused(const LesDom &d, const les_params &prm, int ny, co
     a.ghost = last ? 0 : 1;
     a.rhs = d.sorR;
     a.tj = ny - 4;
-    a.ntiles = ntiles;
+    a.kchunk = kchunk;
+    a.nchunk = nchunk;
+    a.ntiles = tiles * nchunk;
     a.part = d.part;
     a.counter = d.cnt;
     les_launch_sor_iter(d, a, ny, maps, ctx.s);

@@ -15,7 +15,7 @@ struct LesStepPlan {
   LesSorMaps maps;                 // tensor maps of the SOR buffers for sor_ny
 };
 
-int les_step_parts_needed(int im, int jm, int km);
+int les_step_parts_needed(int im, int jm, int km, int sms);
 void les_step_plan_free(LesStepPlan *plan);
 // Queue one step on ctx.s.  Returns 0 or a CUDA error code.
 int les_step_run(const LesDom &d, const les_params &prm, LesStepPlan *plan, int n, int nmax, LesCtx ctx);

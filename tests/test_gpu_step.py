@@ -76,6 +76,31 @@ def test_step_after_uploading_state(built_lib):
             assert np.array_equal(x.view(np.uint32), y.view(np.uint32)), (n, lesgpu.FIELD_NAMES[fid])
 
 
+@pytest.mark.parametrize("kchunk", [3, 5, 8])
+def test_sor_k_chunks_match_one_chunk(built_lib, monkeypatch, kchunk):
+    """The SOR march split into k chunks (each starting with a recomputed red plane)
+    gives the single-chunk result bit for bit; only the residual's summation order
+    differs."""
+    sc = scenario(64, 24, 30, seed=71)
+    params = lesgpu.Params(nmaxp=9)
+
+    def run(chunk):
+        monkeypatch.setenv("LES_SOR_KCHUNK", str(chunk))
+        d = make_gpu(sc, params)
+        for n in range(1, 5):
+            d.step(n, 4)
+        d.sync()
+        return d
+
+    a, b = run(1000), run(kchunk)
+    for fid in lesgpu.STATE_FIELDS:
+        x, y = a.download(fid), b.download(fid)
+        assert np.array_equal(x.view(np.uint32), y.view(np.uint32)), lesgpu.FIELD_NAMES[fid]
+    da, db = a.diag(), b.diag()
+    assert da["iters"] == db["iters"] == 9
+    assert abs(da["sor"] - db["sor"]) <= 1e-6 * abs(da["sor"])
+
+
 @pytest.mark.parametrize("spacing", [(4.0, 4.0), (3.0, 5.0)])
 def test_step_reciprocal_division_matches_ieee(built_lib, monkeypatch, spacing):
     """The reciprocal-corrected divisions (and the power-of-two multiplications) give
