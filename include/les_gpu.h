@@ -93,7 +93,9 @@ typedef struct les_params {
   float omega, pjuge;   /* SOR relaxation and tolerance, press.f95:43-45         */
   int nmaxp;            /* SOR iteration cap, press.f95:44 (50)                  */
   int sor_fixed;        /* 1: always nmaxp iterations; 0: exit on sor < pjuge     */
-  int sor_depth;        /* reserved: pass 0                                       */
+  int sor_ksplit;       /* 0: split the SOR k-march into chunks when the domain's
+                         * tiles leave SMs idle (a domain alone on the GPU); 1: never
+                         * (domains that share the GPU; les_batch_add sets it)    */
 } les_params;
 
 /* Synthetic urban scenario (the configs' generator; replaces the GIS inputs read

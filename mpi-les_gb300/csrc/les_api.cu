@@ -508,6 +508,7 @@ extern "C" int les_gpu_commit_setup(les_handle *h) {
   d.omega = h->prm.omega; d.pjuge = h->prm.pjuge;
   d.logz = logz;
   d.sor_fixed = h->prm.sor_fixed;
+  d.sor_ksplit = h->prm.sor_ksplit;
   d.scal = h->scal_d; d.ctl = h->ctl_d; d.part = h->part_d; d.fscal = h->fscal_d;
   d.sorA = h->sor_d[0]; d.sorB = h->sor_d[1]; d.sorR = h->sor_d[2];
   {  // power-of-two x/y spacings: exact reciprocal multiplications (dvs)
@@ -589,6 +590,16 @@ extern "C" int les_gpu_setup_scenario(les_handle *h, const les_scenario *sc) {
     if (!(h)) return LES_ERR_ARG;                                                          \
     if (!(h)->committed) return fail((h), LES_ERR_STATE, "les_gpu_commit_setup not called"); \
   } while (0)
+
+// Mark a handle as sharing the GPU with other domains (les_batch_add): its SOR march
+// is no longer split in k; a step graph captured with splits is dropped.
+void les_handle_share_gpu(les_handle *h) {
+  if (h->prm.sor_ksplit) return;
+  h->prm.sor_ksplit = 1;
+  h->dom.sor_ksplit = 1;
+  if (h->s) cudaStreamSynchronize(h->s);
+  les_step_plan_free(&h->plan);
+}
 
 // les_noalloc.cu
 int les_noalloc_interior_mean(const LesDom &dom, const float *x, const double *area_dev, cudaStream_t s,

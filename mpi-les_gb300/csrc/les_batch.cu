@@ -11,7 +11,9 @@
 // Calls on one batch are serialised by its mutex.
 //
 // Concurrency across streams is limited by CUDA_DEVICE_MAX_CONNECTIONS (8 unless the
-// process sets it, before CUDA initialises, up to 32).
+// process sets it, before CUDA initialises, up to 32).  Members share the GPU, so
+// joining a batch turns off the k-split of a member's SOR march (les_params.sor_ksplit):
+// the split's ring planes are extra work that pays only on an otherwise idle GPU.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -20,6 +22,9 @@
 #include <vector>
 
 #include "../../include/les_gpu.h"
+
+// les_api.cu: stop splitting the member's SOR march (the GPU is shared)
+void les_handle_share_gpu(les_handle *h);
 
 struct les_batch {
   struct Slot {
@@ -79,6 +84,7 @@ extern "C" int les_batch_add(les_batch *b, les_handle *h, int n0, int nmax, int 
     q = (int)b->slots.size();
     b->slots.emplace_back();
   }
+  les_handle_share_gpu(h);
   b->slots[q].h = h;
   b->slots[q].n = n0;
   b->slots[q].nmax = nmax;

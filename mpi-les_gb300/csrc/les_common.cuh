@@ -64,6 +64,7 @@ struct LesDom {
   float dt, ro, vn, alpha, beta, omega, pjuge;
   float logz;      // alog(0.5*dzn(1)/0.1), vel2.f95:138 and les.f95:133
   int sor_fixed;
+  int sor_ksplit;  // 1: never split the SOR k-march (les_params.sor_ksplit)
   double *scal;    // SC_* slots
   int *ctl;        // CT_* slots
   double *part;    // per-block partial sums

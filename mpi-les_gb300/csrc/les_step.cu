@@ -53,7 +53,7 @@ static void enqueue_sor_fused(const LesDom &d, const les_params &prm, int ny, co
   les_launch_sor_begin(d, ctx);
   const int nit = prm.nmaxp;
   const int tiles = les_sor_fused_tiles(d.im, d.jm, ny);
-  const int kchunk = les_sor_pick_kchunk(tiles, d.km, d.sms > 0 ? d.sms : 152);
+  const int kchunk = d.sor_ksplit ? d.km : les_sor_pick_kchunk(tiles, d.km, d.sms > 0 ? d.sms : 152);
   const int nchunk = (d.km + kchunk - 1) / kchunk;
   for (int l = 1; l <= nit; ++l) {
     SorArgs a;

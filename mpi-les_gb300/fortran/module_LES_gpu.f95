@@ -51,7 +51,7 @@ module module_LES_gpu
   end type
   type, bind(C) :: les_params
     real(c_float) :: dt, ro, vn, alpha, beta, omega, pjuge
-    integer(c_int) :: nmaxp, sor_fixed, sor_depth
+    integer(c_int) :: nmaxp, sor_fixed, sor_ksplit
   end type
 
   type(c_ptr), save :: les_h = c_null_ptr

@@ -71,7 +71,7 @@ class LesDims(C.Structure):
 class LesParams(C.Structure):
     _fields_ = [("dt", C.c_float), ("ro", C.c_float), ("vn", C.c_float), ("alpha", C.c_float),
                 ("beta", C.c_float), ("omega", C.c_float), ("pjuge", C.c_float), ("nmaxp", C.c_int),
-                ("sor_fixed", C.c_int), ("sor_depth", C.c_int)]
+                ("sor_fixed", C.c_int), ("sor_ksplit", C.c_int)]
 
 
 class LesScenario(C.Structure):
@@ -99,11 +99,11 @@ class Params:
     pjuge: float = 1e-4
     nmaxp: int = 50
     sor_fixed: int = 1
-    sor_depth: int = 0
+    sor_ksplit: int = 0  # 1: never split the SOR march in k (domains sharing the GPU)
 
     def to_c(self) -> LesParams:
         return LesParams(self.dt, self.ro, self.vn, self.alpha, self.beta, self.omega, self.pjuge,
-                         self.nmaxp, self.sor_fixed, self.sor_depth)
+                         self.nmaxp, self.sor_fixed, self.sor_ksplit)
 
 
 @dataclasses.dataclass

@@ -74,7 +74,9 @@ class GpuBackend:
         self.lesgpu = lesgpu
         self.batch = lesgpu.Batch()
         self.reserve = reserve_bytes
-        self.params = params or lesgpu.Params()
+        # members share the GPU: their SOR march is never split (graphs captured during
+        # set-up then match the batch's)
+        self.params = params or lesgpu.Params(sor_ksplit=1)
         self.inflight = 0  # bytes of admitted domains whose set-up has not allocated yet
         self.lock = threading.Lock()
 
