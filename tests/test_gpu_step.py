@@ -160,3 +160,21 @@ def test_plain_small_config_vs_fp64(built_lib):
     errs = {nm: rel_err(_interior(gpu, fid, sc, True), _interior(orc, fid, sc, False)) for fid, nm in FIELDS}
     assert max(errs.values()) <= 1e-4, errs
     assert gpu.nonfinite() == 0
+
+
+def test_steps_vs_committed_golden(built_lib):
+    """The solver against the committed oracle fixtures (tests/golden): within 1e-4 of
+    the gfortran-semantics FP32 run and of the FP64 run (the parity contract)."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "oracle_30x20x16_s8.npz"))
+    sc = scenario(30, 20, 16, seed=8)
+    gpu = make_gpu(sc, lesgpu.Params(nmaxp=50))
+    for n in range(1, 4):
+        gpu.step(n, 3)
+    gpu.sync()
+    for fid, nm in FIELDS:
+        x = _interior(gpu, fid, sc, True)
+        for prec in (32, 64):
+            e = rel_err(x, g[f"{nm}{prec}"].astype(np.float64))
+            assert e <= 1e-4, (nm, prec, e)
+    assert gpu.diag()["iters"] == int(g["diag32"][0])
