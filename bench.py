@@ -162,7 +162,7 @@ def reduce_max(pg, x: float) -> float:
     return float(t.item())
 
 
-def cpu_baseline_sample(threads: int | None = None, im=150, jm=150, km=90, steps=3):
+def cpu_baseline_sample(threads: int | None = None, im=150, jm=150, km=90, steps=25):
     """Time the oracle (CPU restatement of les_main's solver) on a bounded sample."""
     import lesgpu
     from oracle import ref as oref
