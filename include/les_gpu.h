@@ -225,6 +225,17 @@ int les_batch_sync(les_batch *b);
 int les_batch_slot(les_batch *b, int slot, int *n, int *nmax);
 int les_batch_last_error(les_batch *b, char *buf, size_t len);
 
+/* Tile shape of press's fused SOR sweep.  nx: float4 columns per tile row, 32 (120
+ * interior i cells) or 16 (56 cells, uniform cn1 only); ny: tile rows, 16/20/24/28
+ * (ny - 4 interior j rows); kchunk: k planes per CTA (the march is split in k chunks
+ * when kchunk < km).  0 leaves a value to the automatic choice.  The shape never
+ * changes the fields, only the speed and the residual's summation order.
+ * les_gpu_set_sor_shape drops captured step graphs (the next step captures again);
+ * les_gpu_sor_shape reports the shape in use, {0, 0, 0} for the per-subroutine SOR
+ * (odd jm or km >= 511).  No reference counterpart: these are the tuning knobs. */
+int les_gpu_set_sor_shape(les_handle *h, int nx, int ny, int kchunk);
+int les_gpu_sor_shape(les_handle *h, int out[3]);
+
 /* Profiling: queue `reps` back-to-back launches of one stage on the handle's stream,
  * bracketed by CUDA events, and return the average milliseconds per repetition.
  * The stage really runs (it advances the state).  what: LES_PROF_*. */

@@ -213,6 +213,7 @@ extern "C" int les_gpu_create(const les_dims *dims, const les_params *params, le
   // partial-sum buffer: the largest per-block count of any reduction kernel
   h->npart = (size_t)std::max<long long>(
       {(long long)((im + 63) / 64) * ((jm + 3) / 4) * km * 2 + 64, (long long)les_step_parts_needed(im, jm, km, h->sms)});
+  h->plan.part_cap = (long long)h->npart;
   // deferred-block lists: [count, ticket, ids...] for the largest grid of those kernels
   {
     const long long fused = (long long)((im + 31) / 32) * ((jm + 1) / 2) * ((km + 3) / 4);
@@ -685,7 +686,7 @@ extern "C" int les_gpu_step(les_handle *h, int n, int nmax) {
   if (h->p_dirty) {
     // p was uploaded: run this step through the per-subroutine kernels, which read p's
     // halos exactly as stored; press leaves them consistent for the fused graph
-    les_step_enqueue(h->dom, h->prm, 0, nullptr, n, ctx_of(h));
+    les_step_enqueue(h->dom, h->prm, SorShape{}, nullptr, n, ctx_of(h));
     h->p_dirty = false;
     return check_launch(h, "step");
   }
@@ -721,6 +722,26 @@ extern "C" int les_gpu_diag(les_handle *h, double out[5]) {
   out[2] = sc[SC_UOUT];
   out[3] = sc[SC_RHSAV];
   out[4] = sc[SC_PAV];
+  return LES_OK;
+}
+
+extern "C" int les_gpu_set_sor_shape(les_handle *h, int nx, int ny, int kchunk) {
+  if (!h) return LES_ERR_ARG;
+  if ((nx != 0 && nx != 16 && nx != 32) || (ny != 0 && ny != 16 && ny != 20 && ny != 24 && ny != 28) || kchunk < 0)
+    return fail(h, LES_ERR_ARG, "set_sor_shape: nx in {0,16,32}, ny in {0,16,20,24,28}, kchunk >= 0");
+  if (h->s) CK(h, cudaStreamSynchronize(h->s));
+  h->plan.fixed = SorShape{nx, ny, kchunk};
+  les_step_plan_free(&h->plan);  // the next step re-plans and captures its graphs again
+  return LES_OK;
+}
+
+extern "C" int les_gpu_sor_shape(les_handle *h, int out[3]) {
+  NEED_COMMIT(h);
+  if (!out) return LES_ERR_ARG;
+  const SorShape sh = les_step_plan_shape(h->dom, &h->plan);
+  out[0] = sh.ny > 0 ? sh.nx : 0;
+  out[1] = sh.ny;
+  out[2] = sh.ny > 0 ? sh.kchunk : 0;
   return LES_OK;
 }
 

@@ -5,8 +5,9 @@
 // cells, boundp1 again; then boundp2 refreshes the k halos.  Within a colour every
 // update reads only cells of the other colour, so a colour is order-free.
 //
-// GB300 mapping.  A CTA owns a tile of 120 (i) x TJ (j) interior cells and marches up
-// k.  Each thread owns one float4 column (4 consecutive i at one j).  At march step s
+// GB300 mapping.  A CTA owns a tile of TI (i) x TJ (j) interior cells and marches up
+// k; TI = 4 NX - 8 with NX = 32 (120 cells) or 16 (56 cells, for narrow domains that
+// share the GPU).  Each thread owns one float4 column (4 consecutive i at one j).  At march step s
 // the CTA relaxes the red cells of plane s and then the black cells of plane s-1
 // (which need the red values of planes s-2, s-1 and s), so one launch performs a whole
 // iteration with one pass over p and rhs.  In-plane j neighbours come from shared
@@ -48,533 +49,9 @@
 
 #include "les_common.cuh"
 #include "les_sor.cuh"
+#include "les_sor_kern.cuh"
 
 namespace {
-
-constexpr int NX = 32;   // float4 columns per tile row: one warp
-constexpr int TI = 120;  // interior i cells per tile (30 float4 columns + 2 ring columns)
-
-__device__ __forceinline__ float f4get(const float4 &v, int e) {
-  return e == 0 ? v.x : e == 1 ? v.y : e == 2 ? v.z : v.w;
-}
-__device__ __forceinline__ void f4set(float4 &v, int e, float x) {
-  if (e == 0) v.x = x; else if (e == 1) v.y = x; else if (e == 2) v.z = x; else v.w = x;
-}
-
-// One relaxation: reltmp = omega*(cn1*(sum of neighbour terms - rhs) - p), left to right.
-__device__ __forceinline__ float relax(float omega, float cn1, float c2l, float pe, float c2s, float pw,
-                                       float c3l, float pn, float c3s, float ps, float c4l, float pu,
-                                       float c4s, float pd, float rhs, float pc) {
-  return omega * (cn1 * (c2l * pe + c2s * pw + c3l * pn + c3s * ps + c4l * pu + c4s * pd - rhs) - pc);
-}
-
-// Relaxation of element E of a float4 (one code path for every lane): the west and
-// east neighbours come from the float4 itself or, at its edges, from the neighbouring
-// columns (pl, pr); at i = 1 and i = im the virtual Neumann halos p(0) = p(1) and
-// p(im+1) = p(im) are selected instead.
-template <int E>
-__device__ __forceinline__ float relax_e(const float4 &cur, float pl, float pr, const float4 &pn,
-                                         const float4 &pso, const float4 &pu, const float4 &pdn,
-                                         const float4 &rr, float rhsav, float omega, float cn1,
-                                         const float (&c2l)[4], const float (&c2s)[4], float c3l, float c3s,
-                                         float c4l, float c4s, bool west_wall, bool east_wall) {
-  const float pc = f4get(cur, E);
-  float pw = (E == 0) ? pl : f4get(cur, E - 1);
-  float pe = (E == 3) ? pr : f4get(cur, E + 1);
-  pw = west_wall ? pc : pw;
-  pe = east_wall ? pc : pe;
-  return relax(omega, cn1, c2l[E], pe, c2s[E], pw, c3l, f4get(pn, E), c3s, f4get(pso, E), c4l,
-               f4get(pu, E), c4s, f4get(pdn, E), f4get(rr, E) - rhsav, pc);
-}
-
-// Red (or black) cells of one float4: e = q and q+2, with q = (j+s) mod 2 (the i of
-// element 0 is odd).  Returns the summed squares of the owned corrections.
-__device__ __forceinline__ float relax_pair(int q, float4 &cur, float pl, float pr, const float4 &pn,
-                                            const float4 &pso, const float4 &pu, const float4 &pdn,
-                                            const float4 &rr, float rhsav, float omega, float cn1,
-                                            const float (&c2l)[4], const float (&c2s)[4], float c3l, float c3s,
-                                            float c4l, float c4s, bool west0, int east_e, bool own,
-                                            const bool (&ival)[4]) {
-  const float4 c = cur;
-  float part;
-  if (q == 0) {
-    const float ra = relax_e<0>(c, pl, pr, pn, pso, pu, pdn, rr, rhsav, omega, cn1, c2l, c2s, c3l, c3s, c4l, c4s, west0, east_e == 0);
-    const float rb = relax_e<2>(c, pl, pr, pn, pso, pu, pdn, rr, rhsav, omega, cn1, c2l, c2s, c3l, c3s, c4l, c4s, false, east_e == 2);
-    cur.x = c.x + ra;
-    cur.z = c.z + rb;
-    part = (own && ival[0] ? ra * ra : 0.f) + (own && ival[2] ? rb * rb : 0.f);
-  } else {
-    const float ra = relax_e<1>(c, pl, pr, pn, pso, pu, pdn, rr, rhsav, omega, cn1, c2l, c2s, c3l, c3s, c4l, c4s, false, east_e == 1);
-    const float rb = relax_e<3>(c, pl, pr, pn, pso, pu, pdn, rr, rhsav, omega, cn1, c2l, c2s, c3l, c3s, c4l, c4s, false, east_e == 3);
-    cur.y = c.y + ra;
-    cur.w = c.w + rb;
-    part = (own && ival[1] ? ra * ra : 0.f) + (own && ival[3] ? rb * rb : 0.f);
-  }
-  return part;
-}
-
-// Per-thread geometry shared by both kernels.
-struct Lane {
-  int c4, r, ib, jr, jw;
-  bool row_owned, row_red, col_owned, owned, west0;
-  int east_e;
-  bool ival[4];
-};
-
-__device__ __forceinline__ Lane make_lane(const LesDom &d, int tj, int ny) {
-  Lane L;
-  L.c4 = threadIdx.x;
-  L.r = threadIdx.y;
-  const int i0 = 1 + blockIdx.x * TI;
-  const int j0 = 1 + blockIdx.y * tj;
-  L.ib = i0 - 4 + 4 * L.c4;
-  L.jr = j0 - 2 + L.r;
-  int jw = (L.jr - 1) % d.jm;
-  if (jw < 0) jw += d.jm;
-  L.jw = jw + 1;
-  L.row_owned = (L.r >= 2) && (L.r <= ny - 3) && (L.jr <= d.jm);
-  L.row_red = (L.r >= 1) && (L.r <= ny - 2);
-  L.col_owned = (L.c4 >= 1) && (L.c4 <= NX - 2);
-  L.owned = L.row_owned && L.col_owned;
-  L.west0 = (L.ib == 1);
-  L.east_e = d.im - L.ib;
-#pragma unroll
-  for (int e = 0; e < 4; ++e) L.ival[e] = (L.ib + e >= 1) && (L.ib + e <= d.im);
-  return L;
-}
-
-// Store the final float4 of plane k (owned cells), plus its periodic ghost rows when
-// the destination is an internal buffer.
-__device__ __forceinline__ void store_final(const LesDom &d, const SorArgs &a, const Lane &L, int k,
-                                            const float4 &v) {
-  auto put = [&](int jrow) {
-    float *dst = a.pdst + (k + LES_KOFF) * d.np + (jrow + LES_JOFF) * d.pi + L.ib + LES_IOFF;
-    if (L.ival[0] && L.ival[3]) {
-      *reinterpret_cast<float4 *>(dst) = v;
-    } else {
-#pragma unroll
-      for (int e = 0; e < 4; ++e)
-        if (L.ival[e]) dst[e] = f4get(v, e);
-    }
-  };
-  put(L.jr);
-  if (a.ghost) {
-    const int jm = d.jm;
-    if (L.jr == 1) put(jm + 1);
-    if (L.jr == 2) put(jm + 2);
-    if (L.jr == jm - 1) put(-1);
-    if (L.jr == jm) put(0);
-  }
-}
-
-// FP32 (Kahan) per thread -> FP64 per CTA -> last CTA sums the CTA partials in order.
-template <int NY>
-__device__ __forceinline__ void finish_residual(const LesDom &d, const SorArgs &a, float acc, double *warp,
-                                                int *last) {
-  const int c4 = threadIdx.x, r = threadIdx.y;
-  float x = acc;
-  for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-  if (c4 == 0) warp[r] = (double)x;
-  __syncthreads();
-  const int cta = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
-  if (r == 0 && c4 == 0) {
-    double t = 0.0;
-    for (int q = 0; q < NY; ++q) t += warp[q];
-    a.part[cta] = t;
-    __threadfence();
-    const unsigned ticket = atomicAdd(a.counter, 1u);
-    *last = (ticket == (unsigned)(a.ntiles - 1));
-  }
-  __syncthreads();
-  if (*last) {
-    __threadfence();
-    const int tid = r * NX + c4;
-    double t = 0.0;
-    for (int q = tid; q < a.ntiles; q += NX * NY) t += ((volatile double *)a.part)[q];
-    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
-    if (c4 == 0) warp[r] = t;
-    __syncthreads();
-    if (tid == 0) {
-      double tot = 0.0;
-      for (int q = 0; q < NY; ++q) tot += warp[q];
-      d.scal[SC_SOR] = tot;
-      d.ctl[CT_ITERS] += 1;
-      if (!d.sor_fixed && tot < (double)d.pjuge) d.ctl[CT_CONVERGED] = 1;
-      *a.counter = 0u;
-    }
-  }
-}
-
-template <int N>
-struct IC {
-  static constexpr int value = N;
-};
-
-// ---------------------------------------------------------------------------------
-// Register kernel: each thread loads its own float4 columns straight into registers,
-// prefetched three march steps ahead.  Reads j ring rows by wrapping, so it runs on p
-// itself (the first iteration) and on any cn1 (uniform, stored or separable).
-template <int NY, int CN1MODE, bool KC>
-__global__ void __launch_bounds__(NX *NY, 1) k_sor_reg(LesDom d, SorArgs a) {
-  __shared__ float4 sOld[2][NY][NX];
-  __shared__ float4 sRed[2][NY][NX];
-  __shared__ float sC4l[LES_SOR_KMAX], sC4s[LES_SOR_KMAX], sCk[LES_SOR_KMAX];
-  __shared__ double sWarp[NY];
-  __shared__ int sLast;
-  if (d.ctl[CT_CONVERGED]) return;  // early exit of press.f95:119-121
-
-  const Lane L = make_lane(d, a.tj, NY);
-  const int c4 = L.c4, r = L.r, ib = L.ib, jw = L.jw;
-  const int im = d.im, jm = d.jm, km = d.km;
-  const bool col_load = (ib <= im + 1);
-  // this CTA's k chunk [ka, kb], marched from ka-1 (a red ring plane) to kb+1
-  const int ka = KC ? 1 + (int)blockIdx.z * a.kchunk : 1;
-  const int kb = KC ? min(km, ka + a.kchunk - 1) : km;
-  const int s_begin = KC ? max(1, ka - 1) : 1;
-  const int s_end = KC ? min(km + 1, kb + 1) : km + 1;
-
-  for (int q = r * NX + c4; q <= km; q += NX * NY) {
-    if (q >= 1) {
-      sC4l[q] = d.gr.cn4l[q];
-      sC4s[q] = d.gr.cn4s[q];
-      sCk[q] = (CN1MODE == 0) ? d.gr.cn1k[q] : d.gr.cn1c[q];
-    }
-  }
-  float c2l[4], c2s[4], cn1a[4];
-#pragma unroll
-  for (int e = 0; e < 4; ++e) {
-    const int i = ib + e;
-    c2l[e] = L.ival[e] ? d.gr.cn2l[i] : 0.f;
-    c2s[e] = L.ival[e] ? d.gr.cn2s[i] : 0.f;
-    cn1a[e] = L.ival[e] ? d.gr.cn1a[i] : 0.f;
-  }
-  const float c3l = d.gr.cn3l[jw], c3s = d.gr.cn3s[jw];
-  const float cn1b = d.gr.cn1b[jw];
-  const float rhsav = d.fscal[SC_RHSAV];
-  const float omega = d.omega;
-  const float *__restrict__ ps = a.psrc;
-  const float *__restrict__ rh = a.rhs;
-  const int colbase = (jw + LES_JOFF) * d.pi + ib + LES_IOFF;  // + (k+1)*np
-  const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
-
-  // plane 0 and plane km+1 are read as planes 1 and km (boundp2's Neumann copies)
-  auto ldp = [&](int k) -> float4 {
-    if (!col_load || k > km + 1) return zero4;
-    const int kk = (k == 0) ? 1 : (k == km + 1) ? km : k;
-    return __ldg(reinterpret_cast<const float4 *>(ps + (kk + LES_KOFF) * d.np + colbase));
-  };
-  auto ldr = [&](int k) -> float4 {
-    if (!col_load || k < 1 || k > km || !L.row_red) return zero4;
-    return __ldg(reinterpret_cast<const float4 *>(rh + (k + LES_KOFF) * d.np + colbase));
-  };
-  auto cn1_at = [&](int e, int k) -> float {
-    if (CN1MODE == 1) return d.cn1[(ib + e - 1) + (jw - 1) * im + (k - 1) * im * jm];
-    return 1.f / (cn1a[e] + cn1b + sCk[k]);
-  };
-
-  // Register rings: plane q of p lives in P[q % 6], plane q of rhs in R[q % 6].  The
-  // march is unrolled 6 times so every slot index is a compile-time constant: the
-  // loads issued for planes s+4 (p) and s+3 (rhs) land in the slots just freed and are
-  // first used three steps later, so their latency overlaps three steps of work.
-  float4 P[6], R[6];
-  if (!KC) {
-    P[0] = ldp(0); P[1] = ldp(1); P[2] = ldp(2); P[3] = ldp(3); P[4] = ldp(4); P[5] = zero4;
-    R[0] = zero4; R[1] = ldr(1); R[2] = ldr(2); R[3] = ldr(3); R[4] = zero4; R[5] = zero4;
-  } else {
-    // planes s_begin-1 .. s_begin+3 of p and s_begin .. s_begin+2 of rhs, in slot plane % 6
-#pragma unroll
-    for (int t = 0; t < 6; ++t) P[t] = R[t] = zero4;
-#pragma unroll
-    for (int q = 0; q < 5; ++q) {
-      const int m = s_begin - 1 + q, slot = m % 6;
-#pragma unroll
-      for (int t = 0; t < 6; ++t)
-        if (t == slot) {
-          P[t] = ldp(m);
-          if (q >= 1 && q <= 3) R[t] = ldr(m);
-        }
-    }
-  }
-  float acc = 0.f, comp = 0.f;
-
-  auto step = [&](auto UC, int s) {
-    constexpr int U = decltype(UC)::value;
-    if (KC && s < s_begin) return;  // before this chunk's start (the unrolled march is aligned to 6)
-    const bool inr = !KC || (s >= ka && s <= kb);  // red of an owned plane (not a ring plane)
-    constexpr int S0 = (1 + U) % 6, SM1 = (S0 + 5) % 6, SM2 = (S0 + 4) % 6, SP1 = (S0 + 1) % 6;
-    constexpr int RP3 = (S0 + 3) % 6;
-    constexpr int B = (1 + U) & 1, BB = U & 1;  // shared-memory parities of planes s, s-1
-    sOld[B][r][c4] = P[S0];
-    __syncthreads();
-    float part = 0.f;
-    const int q = (jw + s) & 1;
-    // ---- red cells of plane s on tile + 1-cell ring
-    // i-neighbours of the float4 edges from the adjacent lanes (a warp is a tile row)
-    const float rpl = __shfl_up_sync(0xffffffffu, P[S0].w, 1);
-    const float rpr = __shfl_down_sync(0xffffffffu, P[S0].x, 1);
-    const float bpl = __shfl_up_sync(0xffffffffu, P[SM1].w, 1);
-    const float bpr = __shfl_down_sync(0xffffffffu, P[SM1].x, 1);
-    if (s <= km && L.row_red) {
-      const float4 pn = sOld[B][r + 1][c4], pso = sOld[B][r - 1][c4];
-      const float pl = rpl, pr = rpr;
-      const float c4l = sC4l[s], c4s = sC4s[s];
-      if (CN1MODE == 0) {
-        part += relax_pair(q, P[S0], pl, pr, pn, pso, P[SP1], P[SM1], R[S0], rhsav, omega, sCk[s], c2l, c2s,
-                           c3l, c3s, c4l, c4s, L.west0, L.east_e, L.owned && inr, L.ival);
-      } else {
-        const float4 cur = P[S0];
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const int i = ib + e;
-          if (!L.ival[e] || ((i + jw + s) & 1) == 0) continue;
-          const float pc = f4get(cur, e);
-          const float pw = (i == 1) ? pc : (e == 0) ? pl : f4get(cur, e - 1);
-          const float pe = (i == im) ? pc : (e == 3) ? pr : f4get(cur, e + 1);
-          const float rt = relax(omega, cn1_at(e, s), c2l[e], pe, c2s[e], pw, c3l, f4get(pn, e), c3s,
-                                 f4get(pso, e), c4l, f4get(P[SP1], e), c4s, f4get(P[SM1], e),
-                                 f4get(R[S0], e) - rhsav, pc);
-          f4set(P[S0], e, pc + rt);
-          if (L.owned && inr) part += rt * rt;
-        }
-      }
-    }
-    sRed[B][r][c4] = P[S0];
-    // ---- black cells of plane s-1 on the tile
-    if ((KC ? (s - 1 >= ka && s - 1 <= kb) : (s >= 2)) && L.owned) {
-      const int k = s - 1;
-      const float4 pn = sRed[BB][r + 1][c4], pso = sRed[BB][r - 1][c4];
-      const float pl = bpl, pr = bpr;
-      const float c4l = sC4l[k], c4s = sC4s[k];
-      if (CN1MODE == 0) {
-        part += relax_pair(q, P[SM1], pl, pr, pn, pso, P[S0], P[SM2], R[SM1], rhsav, omega, sCk[k], c2l, c2s,
-                           c3l, c3s, c4l, c4s, L.west0, L.east_e, true, L.ival);
-      } else {
-        const float4 cur = P[SM1];
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const int i = ib + e;
-          if (!L.ival[e] || ((i + jw + k) & 1) != 0) continue;
-          const float pc = f4get(cur, e);
-          const float pw = (i == 1) ? pc : (e == 0) ? pl : f4get(cur, e - 1);
-          const float pe = (i == im) ? pc : (e == 3) ? pr : f4get(cur, e + 1);
-          const float rt = relax(omega, cn1_at(e, k), c2l[e], pe, c2s[e], pw, c3l, f4get(pn, e), c3s,
-                                 f4get(pso, e), c4l, f4get(P[S0], e), c4s, f4get(P[SM2], e),
-                                 f4get(R[SM1], e) - rhsav, pc);
-          f4set(P[SM1], e, pc + rt);
-          part += rt * rt;
-        }
-      }
-      store_final(d, a, L, k, P[SM1]);
-    }
-    {  // Kahan accumulation of this plane's squared corrections
-      const float y = part - comp;
-      const float t = acc + y;
-      comp = (t - acc) - y;
-      acc = t;
-    }
-    P[SM2] = ldp(s + 4);
-    R[RP3] = ldr(s + 3);
-  };
-
-  for (int s0 = KC ? s_begin - (s_begin - 1) % 6 : 1; s0 <= s_end; s0 += 6) {
-    step(IC<0>{}, s0);
-    if (s0 + 1 > s_end) break;
-    step(IC<1>{}, s0 + 1);
-    if (s0 + 2 > s_end) break;
-    step(IC<2>{}, s0 + 2);
-    if (s0 + 3 > s_end) break;
-    step(IC<3>{}, s0 + 3);
-    if (s0 + 4 > s_end) break;
-    step(IC<4>{}, s0 + 4);
-    if (s0 + 5 > s_end) break;
-    step(IC<5>{}, s0 + 5);
-  }
-  finish_residual<NY>(d, a, acc, sWarp, &sLast);
-}
-
-// ---------------------------------------------------------------------------------
-// TMA kernel: one thread brings each tile plane of p and of rhs into a D-stage shared
-// ring with a single tensor copy apiece (cp.async.bulk.tensor, 128 x NY floats),
-// signalled by an mbarrier, D-2 march steps ahead of first use.  Needs a source with
-// periodic ghost rows (an internal buffer) and a uniform cn1.  Waits are bounded: if
-// a stage never arrives the CTA stops computing, sets CT_ERROR and still meets every
-// barrier, then waits (bounded) for the copies it issued.
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// bounded wait: gives up after 2^20 polls (each poll may itself suspend briefly)
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-  for (int it = 0; it < (1 << 20); ++it)
-    if (mbar_try_wait(bar, parity)) return true;
-  return false;
-}
-__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int x, int y, int z, uint64_t *bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
-      "[%5];" ::"r"(smem_u32(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
-      : "memory");
-}
-
-template <int NY, int D>
-struct TmaSmem {
-  float4 p[D][NY][NX];    // old planes of p (tile + 2-cell ring)
-  float4 rhs[D][NY][NX];  // planes of rhs
-  float4 red[2][NY][NX];  // red-updated planes
-  float c4l[LES_SOR_KMAX], c4s[LES_SOR_KMAX], ck[LES_SOR_KMAX];
-  uint64_t bar[D];
-  double warp[NY];
-  int last, abort_;
-};
-
-template <int NY, int D, bool KC>
-__global__ void __launch_bounds__(NX *NY, 1)
-    k_sor_tma(LesDom d, SorArgs a, const __grid_constant__ CUtensorMap tmP, const __grid_constant__ CUtensorMap tmR) {
-  extern __shared__ __align__(1024) unsigned char smem_raw[];
-  TmaSmem<NY, D> &S = *reinterpret_cast<TmaSmem<NY, D> *>(smem_raw);
-  if (d.ctl[CT_CONVERGED]) return;  // early exit of press.f95:119-121
-
-  const Lane L = make_lane(d, a.tj, NY);
-  const int c4 = L.c4, r = L.r, ib = L.ib, jw = L.jw;
-  const int km = d.km;
-  float c2l[4], c2s[4];
-#pragma unroll
-  for (int e = 0; e < 4; ++e) {
-    c2l[e] = L.ival[e] ? d.gr.cn2l[ib + e] : 0.f;
-    c2s[e] = L.ival[e] ? d.gr.cn2s[ib + e] : 0.f;
-  }
-  const float c3l = d.gr.cn3l[jw], c3s = d.gr.cn3s[jw];
-  const float rhsav = d.fscal[SC_RHSAV];
-  const float omega = d.omega;
-  const bool producer = (r == 0) && (c4 == 0);
-  const int tx = blockIdx.x * TI;   // padded column of i0 - 4
-  const int ty = blockIdx.y * a.tj; // padded row of j0 - 2
-  const uint32_t stage_bytes = 2u * NY * NX * 16u;
-  // this CTA's k chunk [ka, kb], marched from ka-1 (a red ring plane) to kb+1; it
-  // loads planes mfirst .. mlast, plane m into stage (m - mfirst) % D
-  const int ka = KC ? 1 + (int)blockIdx.z * a.kchunk : 1;
-  const int kb = KC ? min(km, ka + a.kchunk - 1) : km;
-  const int s_begin = KC ? max(1, ka - 1) : 1;
-  const int s_end = KC ? min(km + 1, kb + 1) : km + 1;
-  const int mfirst = KC ? max(1, s_begin - 1) : 1;
-  const int mlast = KC ? min(km, kb + 2) : km;
-  auto issue = [&](int m) {  // plane m (mfirst..mlast) into stage (m - mfirst) % D
-    const int q = (m - mfirst) % D;
-    mbar_expect_tx(&S.bar[q], stage_bytes);
-    tma_load_3d(&S.p[q][0][0], &tmP, tx, ty, m + LES_KOFF, &S.bar[q]);
-    tma_load_3d(&S.rhs[q][0][0], &tmR, tx, ty, m + LES_KOFF, &S.bar[q]);
-  };
-
-  if (producer) {
-    for (int q = 0; q < D; ++q) mbar_init(&S.bar[q], 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    S.abort_ = 0;
-  }
-  for (int q = r * NX + c4; q <= km; q += NX * NY) {
-    if (q >= 1) {
-      S.c4l[q] = d.gr.cn4l[q];
-      S.c4s[q] = d.gr.cn4s[q];
-      S.ck[q] = d.gr.cn1k[q];
-    }
-  }
-  __syncthreads();
-  if (producer)
-    for (int m = mfirst; m < mfirst + D && m <= mlast; ++m) issue(m);
-
-  int failed_at = 0;
-  auto wait_plane = [&](int m) {
-    if (!mbar_wait(&S.bar[(m - mfirst) % D], (uint32_t)(((m - mfirst) / D) & 1))) {
-      S.abort_ = 1;
-      d.ctl[CT_ERROR] = 1;
-      if (!failed_at) failed_at = m;
-    }
-  };
-
-  const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
-  float4 Pm2 = zero4, Pm1 = zero4, P0 = zero4, Rm1 = zero4;
-  if (KC && s_begin > 1) {
-    wait_plane(s_begin - 1);
-    Pm1 = S.p[(s_begin - 1 - mfirst) % D][r][c4];
-  }
-  wait_plane(s_begin);
-  P0 = S.p[(s_begin - mfirst) % D][r][c4];
-  float acc = 0.f, comp = 0.f;
-
-  for (int s = s_begin; s <= s_end; ++s) {
-    __syncthreads();
-    if (S.abort_) continue;
-    // the stage of plane s-1 is free: every thread has left step s-1 (or the prologue)
-    if (producer && s - 1 >= mfirst && s - 1 + D <= mlast) issue(s - 1 + D);
-    float4 P1 = P0, R0 = zero4;
-    if (s + 1 <= mlast) {
-      wait_plane(s + 1);
-      P1 = S.p[(s + 1 - mfirst) % D][r][c4];
-    }
-    float part = 0.f;
-    const int B = s & 1, BB = (s - 1) & 1;
-    const int q = (jw + s) & 1;
-    // i-neighbours of the float4 edges from the adjacent lanes (a warp is a tile row)
-    const float rpl = __shfl_up_sync(0xffffffffu, P0.w, 1);
-    const float rpr = __shfl_down_sync(0xffffffffu, P0.x, 1);
-    const float bpl = __shfl_up_sync(0xffffffffu, Pm1.w, 1);
-    const float bpr = __shfl_down_sync(0xffffffffu, Pm1.x, 1);
-    if (s <= km && L.row_red) {
-      const int st = (s - mfirst) % D;
-      R0 = S.rhs[st][r][c4];
-      const float4 pn = S.p[st][r + 1][c4], pso = S.p[st][r - 1][c4];
-      const float pl = rpl, pr = rpr;
-      // virtual k halos: p(0) = p(1), p(km+1) = p(km) (the cell's own value)
-      const float4 up = (s == km) ? P0 : P1;
-      const float4 dn = (s == 1) ? P0 : Pm1;
-      part += relax_pair(q, P0, pl, pr, pn, pso, up, dn, R0, rhsav, omega, S.ck[s], c2l, c2s, c3l, c3s,
-                         S.c4l[s], S.c4s[s], L.west0, L.east_e, L.owned && (!KC || (s >= ka && s <= kb)), L.ival);
-    }
-    S.red[B][r][c4] = P0;
-    if ((KC ? (s - 1 >= ka && s - 1 <= kb) : (s >= 2)) && L.owned) {
-      const int k = s - 1;
-      const float4 pn = S.red[BB][r + 1][c4], pso = S.red[BB][r - 1][c4];
-      const float pl = bpl, pr = bpr;
-      const float4 up = (k == km) ? Pm1 : P0;
-      const float4 dn = (k == 1) ? Pm1 : Pm2;
-      part += relax_pair(q, Pm1, pl, pr, pn, pso, up, dn, Rm1, rhsav, omega, S.ck[k], c2l, c2s, c3l, c3s,
-                         S.c4l[k], S.c4s[k], L.west0, L.east_e, true, L.ival);
-      store_final(d, a, L, k, Pm1);
-    }
-    {
-      const float y = part - comp;
-      const float t = acc + y;
-      comp = (t - acc) - y;
-      acc = t;
-    }
-    Pm2 = Pm1;
-    Pm1 = P0;
-    P0 = P1;
-    Rm1 = R0;
-  }
-  // after a failed wait, wait (bounded) for the copies already issued before leaving
-  if (failed_at) {
-    for (int m = failed_at; m <= mlast && m < failed_at + D; ++m)
-      (void)mbar_wait(&S.bar[(m - mfirst) % D], (uint32_t)(((m - mfirst) / D) & 1));
-  }
-  finish_residual<NY>(d, a, acc, S.warp, &S.last);
-}
 
 // Copy the interior of the buffer the last executed iteration wrote back into p, when
 // the sweep stopped before its final (p-writing) iteration.
@@ -592,52 +69,48 @@ __global__ void k_sor_copyout(LesDom d, int nmaxp) {
   }
 }
 
-template <int NY, bool KC>
-void launch_reg_kc(const LesDom &d, const SorArgs &a, int cn1mode, cudaStream_t s) {
-  const dim3 grid((d.im + TI - 1) / TI, (d.jm + a.tj - 1) / a.tj, KC ? a.nchunk : 1);
-  const dim3 block(NX, NY);
-  if (cn1mode == 1) k_sor_reg<NY, 1, KC><<<grid, block, 0, s>>>(d, a);
-  else if (cn1mode == 2) k_sor_reg<NY, 2, KC><<<grid, block, 0, s>>>(d, a);
-  else k_sor_reg<NY, 0, KC><<<grid, block, 0, s>>>(d, a);
-}
 template <int NY>
 void launch_reg(const LesDom &d, const SorArgs &a, int cn1mode, cudaStream_t s) {
-  if (a.nchunk > 1) launch_reg_kc<NY, true>(d, a, cn1mode, s);
-  else launch_reg_kc<NY, false>(d, a, cn1mode, s);
-}
-
-template <int NY, int D, bool KC>
-void launch_tma_kc(const LesDom &d, const SorArgs &a, const CUtensorMap &tp, const CUtensorMap &tr, cudaStream_t s) {
-  const dim3 grid((d.im + TI - 1) / TI, (d.jm + a.tj - 1) / a.tj, KC ? a.nchunk : 1);
-  const size_t bytes = sizeof(TmaSmem<NY, D>);
-  cudaFuncSetAttribute(k_sor_tma<NY, D, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-  k_sor_tma<NY, D, KC><<<grid, dim3(NX, NY), bytes, s>>>(d, a, tp, tr);
+  if (a.nchunk > 1) launch_reg_kc<32, NY, true>(d, a, cn1mode, s);
+  else launch_reg_kc<32, NY, false>(d, a, cn1mode, s);
 }
 template <int NY, int D>
 void launch_tma(const LesDom &d, const SorArgs &a, const CUtensorMap &tp, const CUtensorMap &tr, cudaStream_t s) {
-  if (a.nchunk > 1) launch_tma_kc<NY, D, true>(d, a, tp, tr, s);
-  else launch_tma_kc<NY, D, false>(d, a, tp, tr, s);
+  if (a.nchunk > 1) launch_tma_kc<32, NY, D, true>(d, a, tp, tr, s);
+  else launch_tma_kc<32, NY, D, false>(d, a, tp, tr, s);
 }
 
 }  // namespace
 
-int les_sor_fused_tiles(int im, int jm, int ny) {
-  const int tj = ny - 4;
-  return ((im + TI - 1) / TI) * ((jm + tj - 1) / tj);
+int les_sor_fused_tiles(int im, int jm, SorShape sh) {
+  const int ti = 4 * sh.nx - 8, tj = sh.ny - 4;
+  return ((im + ti - 1) / ti) * ((jm + tj - 1) / tj);
 }
 
-int les_sor_pick_ny(int im, int jm, int sms) {
-  // Each CTA holds one SM.  Pick the tile height whose CTA count fills the SMs in the
-  // fewest waves, preferring less ring overhead on ties.
-  static const int cands[] = {16, 20, 24, 28};
-  int best = 24;
+SorShape les_sor_pick_shape(int im, int jm, int sms, bool shared_gpu) {
+  static const int nys[] = {16, 20, 24, 28};
+  SorShape best{32, 24};
   double best_cost = 1e30;
-  for (int ny : cands) {
-    const int tiles = les_sor_fused_tiles(im, jm, ny);
-    const int waves = (tiles + sms - 1) / sms;
-    const double cost = waves * (double)ny;
-    if (cost < best_cost - 1e-9) { best_cost = cost; best = ny; }
+  if (!shared_gpu) {
+    // A domain alone: each 32-column CTA holds one SM.  Pick the tile height whose
+    // CTA count fills the SMs in the fewest waves, preferring less ring overhead on
+    // ties (the k-split then fills the SMs that are still idle).
+    for (int ny : nys) {
+      const int tiles = les_sor_fused_tiles(im, jm, SorShape{32, ny});
+      const double cost = ((tiles + sms - 1) / sms) * (double)ny;
+      if (cost < best_cost - 1e-9) { best_cost = cost; best = SorShape{32, ny}; }
+    }
+    return best;
   }
+  // A domain sharing the GPU with others: the SMs stay busy, so the cost is the
+  // thread-planes the launch issues, ring columns and rows included (tiles x NX x NY).
+  // 16-column tiles waste fewer ring and padding columns on narrow domains.
+  for (int nx : {32, 16})
+    for (int ny : nys) {
+      const SorShape sh{nx, ny};
+      const double cost = (double)les_sor_fused_tiles(im, jm, sh) * nx * ny;
+      if (cost < best_cost - 1e-9) { best_cost = cost; best = sh; }
+    }
   return best;
 }
 
@@ -652,7 +125,7 @@ int les_sor_pick_kchunk(int tiles, int km, int sms) {
   return (km + nch - 1) / nch;
 }
 
-int les_sor_make_maps(const LesDom &d, int ny, LesSorMaps *maps) {
+int les_sor_make_maps(const LesDom &d, SorShape sh, LesSorMaps *maps) {
   using EncodeFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
                                 const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -667,7 +140,7 @@ int les_sor_make_maps(const LesDom &d, int ny, LesSorMaps *maps) {
   }
   const cuuint64_t dims[3] = {(cuuint64_t)d.pi, (cuuint64_t)d.nj, (cuuint64_t)(d.km + 4)};
   const cuuint64_t strides[2] = {(cuuint64_t)d.pi * 4u, (cuuint64_t)d.np * 4u};
-  const cuuint32_t box[3] = {(cuuint32_t)(NX * 4), (cuuint32_t)ny, 1u};
+  const cuuint32_t box[3] = {(cuuint32_t)(sh.nx * 4), (cuuint32_t)sh.ny, 1u};
   const cuuint32_t estr[3] = {1u, 1u, 1u};
   float *bases[3] = {d.sorA, d.sorB, d.sorR};
   for (int q = 0; q < 3; ++q) {
@@ -676,31 +149,35 @@ int les_sor_make_maps(const LesDom &d, int ny, LesSorMaps *maps) {
                          CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (rc != CUDA_SUCCESS) return -2;
   }
-  maps->ny = ny;
+  maps->shape = sh;
   maps->valid = 1;
   return 0;
 }
 
-void les_launch_sor_iter(const LesDom &d, const SorArgs &a, int ny, const LesSorMaps *maps, cudaStream_t s) {
+void les_launch_sor_iter(const LesDom &d, const SorArgs &a, SorShape sh, const LesSorMaps *maps, cudaStream_t s) {
   const int cn1mode = d.gr.cn1k ? 0 : (d.cn1 ? 1 : 2);
   // LES_SOR_KIND=0 forces the register kernel everywhere (A/B measurements)
   static const int kind = [] {
     const char *e = getenv("LES_SOR_KIND");
     return e ? atoi(e) : 1;
   }();
-  const bool tma = kind != 0 && maps && maps->valid && maps->ny == ny && cn1mode == 0 &&
-                   (a.psrc == d.sorA || a.psrc == d.sorB);
+  const bool tma = kind != 0 && maps && maps->valid && maps->shape.nx == sh.nx && maps->shape.ny == sh.ny &&
+                   cn1mode == 0 && (a.psrc == d.sorA || a.psrc == d.sorB);
+  const CUtensorMap *tp = tma ? ((a.psrc == d.sorA) ? &maps->m[0] : &maps->m[1]) : nullptr;
+  const CUtensorMap *tr = tma ? &maps->m[2] : nullptr;
+  if (sh.nx == 16) {
+    les_launch_sor_iter_nx16(d, a, sh.ny, tp, tr, s);
+    return;
+  }
   if (tma) {
-    const CUtensorMap &tp = (a.psrc == d.sorA) ? maps->m[0] : maps->m[1];
-    const CUtensorMap &tr = maps->m[2];
-    switch (ny) {
-      case 16: launch_tma<16, 6>(d, a, tp, tr, s); return;
-      case 20: launch_tma<20, 6>(d, a, tp, tr, s); return;
-      case 28: launch_tma<28, 4>(d, a, tp, tr, s); return;
-      default: launch_tma<24, 6>(d, a, tp, tr, s); return;
+    switch (sh.ny) {
+      case 16: launch_tma<16, 6>(d, a, *tp, *tr, s); return;
+      case 20: launch_tma<20, 6>(d, a, *tp, *tr, s); return;
+      case 28: launch_tma<28, 4>(d, a, *tp, *tr, s); return;
+      default: launch_tma<24, 6>(d, a, *tp, *tr, s); return;
     }
   }
-  switch (ny) {
+  switch (sh.ny) {
     case 16: launch_reg<16>(d, a, cn1mode, s); break;
     case 20: launch_reg<20>(d, a, cn1mode, s); break;
     case 28: launch_reg<28>(d, a, cn1mode, s); break;

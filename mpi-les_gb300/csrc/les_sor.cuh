@@ -12,7 +12,7 @@ struct SorArgs {
   const float *psrc;     // p at the start of the iteration (read only)
   float *pdst;           // p at the end of the iteration (interior written)
   const float *rhs;      // rhs before the rhsav shift (the sweep subtracts rhsav)
-  int tj;                // interior rows per tile (tile height NY - 4)
+  int tj;                // interior rows per tile (tile height ny - 4)
   int ntiles;            // CTAs in the launch
   double *part;          // per-CTA residual partials (>= ntiles)
   unsigned int *counter; // CTA completion ticket, zero between launches
@@ -21,20 +21,33 @@ struct SorArgs {
   int nchunk;            // chunks (grid z)
 };
 
-// Tensor maps of the internal buffers (sorA, sorB, sorR) for one tile height.
+// Tile shape of the fused sweep: nx float4 columns (32 or 16; the interior i cells per
+// tile are 4 nx - 8) by ny rows (the interior j rows are ny - 4), and kchunk k planes
+// per CTA (>= km: the whole march).  ny == 0 selects the per-subroutine path instead.
+struct SorShape {
+  int nx = 0, ny = 0, kchunk = 0;
+};
+
+// Tensor maps of the internal buffers (sorA, sorB, sorR) for one tile shape.
 struct LesSorMaps {
   CUtensorMap m[3];
-  int ny = 0;
+  SorShape shape;
   int valid = 0;
 };
 
-int les_sor_fused_tiles(int im, int jm, int ny);
-int les_sor_pick_ny(int im, int jm, int sms);
+int les_sor_fused_tiles(int im, int jm, SorShape sh);
+// The tile shape for a domain alone on the GPU (fewest waves of one-SM CTAs) or
+// sharing it with other domains (fewest thread-planes, ring cells included).
+SorShape les_sor_pick_shape(int im, int jm, int sms, bool shared_gpu);
 // Planes per k chunk: one chunk when the tiles fill the SMs, else enough chunks to
 // fill them (each at least 8 planes: a chunk recomputes one red plane below it).
 int les_sor_pick_kchunk(int tiles, int km, int sms);
-int les_sor_make_maps(const LesDom &d, int ny, LesSorMaps *maps);
+int les_sor_make_maps(const LesDom &d, SorShape sh, LesSorMaps *maps);
 // One SOR iteration: the TMA kernel when the source is an internal buffer with valid
 // maps and cn1 is uniform, the register kernel otherwise.
-void les_launch_sor_iter(const LesDom &d, const SorArgs &a, int ny, const LesSorMaps *maps, cudaStream_t s);
+void les_launch_sor_iter(const LesDom &d, const SorArgs &a, SorShape sh, const LesSorMaps *maps, cudaStream_t s);
+// 16-column tiles (les_sor16.cu): the TMA kernel when tp and tr are given, the register
+// kernel (uniform cn1, one k chunk) otherwise.
+void les_launch_sor_iter_nx16(const LesDom &d, const SorArgs &a, int ny, const CUtensorMap *tp,
+                              const CUtensorMap *tr, cudaStream_t s);
 void les_launch_sor_copyout(const LesDom &d, int nmaxp, cudaStream_t s);

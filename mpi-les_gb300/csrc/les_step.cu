@@ -16,12 +16,13 @@
 
 int les_step_parts_needed(int im, int jm, int km, int sms) {
   int worst = 0;
-  for (int ny = 16; ny <= 32; ny += 4) {
-    const int t = les_sor_fused_tiles(im, jm, ny);
-    const int kc = les_sor_pick_kchunk(t, km, sms > 0 ? sms : 152);
-    const int parts = t * ((km + kc - 1) / kc);
-    worst = parts > worst ? parts : worst;
-  }
+  for (int nx : {32, 16})
+    for (int ny = 16; ny <= 28; ny += 4) {
+      const int t = les_sor_fused_tiles(im, jm, SorShape{nx, ny});
+      const int kc = les_sor_pick_kchunk(t, km, sms > 0 ? sms : 152);
+      const int parts = t * ((km + kc - 1) / kc);
+      worst = parts > worst ? parts : worst;
+    }
   return worst + 64;
 }
 
@@ -31,29 +32,64 @@ void les_step_plan_free(LesStepPlan *plan) {
     plan->exec[q] = nullptr;
     plan->launches[q] = 0;
   }
-  plan->sor_ny = 0;
+  plan->sor = SorShape{};
+  plan->sor_picked = 0;
   plan->maps.valid = 0;
 }
 
-int les_step_pick_ny(const LesDom &d) {
-  if (d.jm % 2 != 0) return 0;            // the wrapped j ring needs an even jm
-  if (d.km + 1 >= LES_SOR_KMAX) return 0;  // per-k coefficients staged in shared memory
+SorShape les_step_pick_shape(const LesDom &d) {
+  if (d.jm % 2 != 0) return SorShape{};            // the wrapped j ring needs an even jm
+  if (d.km + 1 >= LES_SOR_KMAX) return SorShape{};  // per-k coefficients staged in shared memory
+  SorShape sh = les_sor_pick_shape(d.im, d.jm, d.sms > 0 ? d.sms : 152, d.sor_ksplit != 0);
+  // A/B measurements: LES_SOR_NX (32, 16), LES_SOR_NY (16, 20, 24, 28)
+  if (const char *e = getenv("LES_SOR_NX")) {
+    const int v = atoi(e);
+    if (v == 16 || v == 32) sh.nx = v;
+  }
   if (const char *e = getenv("LES_SOR_NY")) {
     const int v = atoi(e);
-    if (v == 16 || v == 20 || v == 24 || v == 28 || v == 32) return v;
+    if (v == 16 || v == 20 || v == 24 || v == 28) sh.ny = v;
   }
-  return les_sor_pick_ny(d.im, d.jm, d.sms > 0 ? d.sms : 152);
+  if (!d.gr.cn1k) sh.nx = 32;  // 16-column tiles are built for a uniform cn1 only
+  return sh;
+}
+
+static void plan_pick(const LesDom &d, LesStepPlan *plan) {
+  if (plan->sor_picked) return;
+  SorShape sh = les_step_pick_shape(d);
+  if (sh.ny > 0) {
+    if (plan->fixed.nx && (plan->fixed.nx == 32 || d.gr.cn1k)) sh.nx = plan->fixed.nx;
+    if (plan->fixed.ny) sh.ny = plan->fixed.ny;
+    const int tiles = les_sor_fused_tiles(d.im, d.jm, sh);
+    // 16-column tiles march the whole k range (no k-chunk kernels are built for them)
+    int kc = d.km;
+    if (sh.nx == 32 && plan->fixed.kchunk > 0) kc = plan->fixed.kchunk;
+    else if (sh.nx == 32 && !d.sor_ksplit) kc = les_sor_pick_kchunk(tiles, d.km, d.sms > 0 ? d.sms : 152);
+    kc = kc < 1 ? 1 : (kc > d.km ? d.km : kc);
+    if (plan->part_cap > 0 && (long long)tiles * ((d.km + kc - 1) / kc) > plan->part_cap) kc = d.km;
+    sh.kchunk = kc;
+  }
+  plan->sor = sh;
+  plan->maps.valid = 0;
+  if (sh.ny > 0 && les_sor_make_maps(d, sh, &plan->maps) != 0) plan->maps.valid = 0;
+  plan->sor_picked = 1;
+}
+
+SorShape les_step_plan_shape(const LesDom &d, LesStepPlan *plan) {
+  plan_pick(d, plan);
+  return plan->sor;
 }
 
 // Iteration l reads p (l = 1) or the internal buffer iteration l-1 wrote, and writes
 // the internal buffer X(l) (X = sorB for odd l, sorA for even l) or, for the last
 // iteration, p itself.  A copy-out moves the result into p when the sweep stopped
 // early (press.f95:119) or ran a single iteration.
-static void enqueue_sor_fused(const LesDom &d, const les_params &prm, int ny, const LesSorMaps *maps, LesCtx ctx) {
+static void enqueue_sor_fused(const LesDom &d, const les_params &prm, SorShape sh, const LesSorMaps *maps,
+                              LesCtx ctx) {
   les_launch_sor_begin(d, ctx);
   const int nit = prm.nmaxp;
-  const int tiles = les_sor_fused_tiles(d.im, d.jm, ny);
-  const int kchunk = d.sor_ksplit ? d.km : les_sor_pick_kchunk(tiles, d.km, d.sms > 0 ? d.sms : 152);
+  const int tiles = les_sor_fused_tiles(d.im, d.jm, sh);
+  const int kchunk = sh.kchunk > 0 ? sh.kchunk : d.km;
   const int nchunk = (d.km + kchunk - 1) / kchunk;
   for (int l = 1; l <= nit; ++l) {
     SorArgs a;
@@ -62,28 +98,28 @@ static void enqueue_sor_fused(const LesDom &d, const les_params &prm, int ny, co
     a.pdst = last ? d.p : ((l & 1) ? d.sorB : d.sorA);
     a.ghost = last ? 0 : 1;
     a.rhs = d.sorR;
-    a.tj = ny - 4;
+    a.tj = sh.ny - 4;
     a.kchunk = kchunk;
     a.nchunk = nchunk;
     a.ntiles = tiles * nchunk;
     a.part = d.part;
     a.counter = d.cnt;
-    les_launch_sor_iter(d, a, ny, maps, ctx.s);
+    les_launch_sor_iter(d, a, sh, maps, ctx.s);
     ++*ctx.nlaunch;
   }
   les_launch_sor_copyout(d, nit, ctx.s);
   ++*ctx.nlaunch;
 }
 
-void les_step_enqueue(const LesDom &d, const les_params &prm, int ny, const LesSorMaps *maps, int n, LesCtx ctx) {
+void les_step_enqueue(const LesDom &d, const les_params &prm, SorShape sh, const LesSorMaps *maps, int n, LesCtx ctx) {
   les_launch_velnw(d, ctx);
   les_launch_bondv1(d, n, ctx);
   les_launch_velfg_fused(d, true, ctx);  // velfg + feedbf
   les_launch_les_fused(d, true, ctx);    // les + adam
   les_launch_bondfg(d, ctx);
-  if (ny > 0) {
+  if (sh.ny > 0) {
     les_launch_rhs_sor(d, ctx);
-    enqueue_sor_fused(d, prm, ny, maps, ctx);
+    enqueue_sor_fused(d, prm, sh, maps, ctx);
   } else {
     les_launch_rhs_mean(d, ctx);
     les_launch_sor_simple(d, prm.nmaxp, ctx);
@@ -95,16 +131,13 @@ int les_step_run(const LesDom &d, const les_params &prm, LesStepPlan *plan, int 
   (void)nmax;
   const int q = (n == 1) ? 0 : 1;
   if (!plan->exec[q]) {
-    if (plan->sor_ny == 0) {
-      plan->sor_ny = les_step_pick_ny(d);
-      if (plan->sor_ny > 0 && les_sor_make_maps(d, plan->sor_ny, &plan->maps) != 0) plan->maps.valid = 0;
-    }
+    plan_pick(d, plan);
     cudaGraph_t g = nullptr;
     long long cnt = 0;
     LesCtx cap{ctx.s, &cnt};
     cudaError_t e = cudaStreamBeginCapture(ctx.s, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return (int)e;
-    les_step_enqueue(d, prm, plan->sor_ny, &plan->maps, n, cap);
+    les_step_enqueue(d, prm, plan->sor, &plan->maps, n, cap);
     e = cudaStreamEndCapture(ctx.s, &g);
     if (e != cudaSuccess) return (int)e;
     e = cudaGraphInstantiate(&plan->exec[q], g, 0);
@@ -122,19 +155,15 @@ int les_step_run(const LesDom &d, const les_params &prm, LesStepPlan *plan, int 
 }
 
 int les_step_sor_pass(const LesDom &d, const les_params &prm, LesStepPlan *plan, LesCtx ctx) {
-  if (plan->sor_ny == 0) {
-    plan->sor_ny = les_step_pick_ny(d);
-    if (plan->sor_ny > 0 && les_sor_make_maps(d, plan->sor_ny, &plan->maps) != 0) plan->maps.valid = 0;
-  }
-  const int ny = plan->sor_ny;
-  if (ny == 0) {
+  plan_pick(d, plan);
+  if (plan->sor.ny == 0) {
     les_launch_sor_simple(d, 1, ctx);
     return 1;
   }
   // ten iterations as the step runs them: the first reads p, the last writes p
   les_params ten = prm;
   ten.nmaxp = 10;
-  enqueue_sor_fused(d, ten, ny, &plan->maps, ctx);
+  enqueue_sor_fused(d, ten, plan->sor, &plan->maps, ctx);
   return 10;
 }
 void les_step_velfg_pass(const LesDom &d, LesCtx ctx) { les_launch_velfg_fused(d, true, ctx); }

@@ -11,8 +11,12 @@
 struct LesStepPlan {
   cudaGraphExec_t exec[2] = {nullptr, nullptr};
   long long launches[2] = {0, 0};  // kernels inside each graph
-  int sor_ny = 0;                  // fused SOR tile height (warps per CTA), 0 = simple path
-  LesSorMaps maps;                 // tensor maps of the SOR buffers for sor_ny
+  SorShape sor;                    // fused SOR tile shape (sor.ny == 0: per-subroutine path)
+  int sor_picked = 0;              // sor chosen (and maps made) for this plan
+  LesSorMaps maps;                 // tensor maps of the SOR buffers for sor
+  SorShape fixed;                  // caller's choice (les_gpu_set_sor_shape), 0 = automatic;
+                                   // kept across les_step_plan_free
+  long long part_cap = 0;          // residual partials the domain's buffer holds
 };
 
 int les_step_parts_needed(int im, int jm, int km, int sms);
@@ -21,8 +25,11 @@ void les_step_plan_free(LesStepPlan *plan);
 int les_step_run(const LesDom &d, const les_params &prm, LesStepPlan *plan, int n, int nmax, LesCtx ctx);
 // Single passes of the step's heavy kernels, for profiling (les_gpu_profile).
 int les_step_sor_pass(const LesDom &d, const les_params &prm, LesStepPlan *plan, LesCtx ctx);  // iterations run
-int les_step_pick_ny(const LesDom &d);
+SorShape les_step_pick_shape(const LesDom &d);
+// The plan's SOR shape (picked on first use): the automatic choice with the fixed
+// parts applied.
+SorShape les_step_plan_shape(const LesDom &d, LesStepPlan *plan);
 void les_step_velfg_pass(const LesDom &d, LesCtx ctx);
 void les_step_les_pass(const LesDom &d, LesCtx ctx);
 // The launch sequence itself (no graph), used for capture and by tests.
-void les_step_enqueue(const LesDom &d, const les_params &prm, int ny, const LesSorMaps *maps, int n, LesCtx ctx);
+void les_step_enqueue(const LesDom &d, const les_params &prm, SorShape sh, const LesSorMaps *maps, int n, LesCtx ctx);

@@ -180,6 +180,8 @@ def load_library(path: str | None = None) -> C.CDLL:
         "les_gpu_launch_count": (C.c_longlong, [vp]),
         "les_gpu_last_error": (C.c_int, [vp, C.c_char_p, C.c_size_t]),
         "les_gpu_profile": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(C.c_double)]),
+        "les_gpu_set_sor_shape": (C.c_int, [vp, C.c_int, C.c_int, C.c_int]),
+        "les_gpu_sor_shape": (C.c_int, [vp, C.POINTER(C.c_int)]),
         "les_batch_create": (C.c_int, [C.POINTER(vp)]),
         "les_batch_destroy": (C.c_int, [vp]),
         "les_batch_admit": (C.c_int, [C.POINTER(LesDims), C.c_size_t, ip_]),
@@ -356,6 +358,16 @@ class Domain:
         s = C.c_void_p()
         self._check(self.lib.les_gpu_stream(self._h, C.byref(s)), "stream")
         return s.value or 0
+
+    def set_sor_shape(self, nx: int = 0, ny: int = 0, kchunk: int = 0) -> None:
+        """Fix the SOR sweep's tile shape (0 = automatic); see les_gpu_set_sor_shape."""
+        self._check(self.lib.les_gpu_set_sor_shape(self._h, nx, ny, kchunk), "set_sor_shape")
+
+    def sor_shape(self) -> tuple[int, int, int]:
+        """(nx, ny, kchunk) of the SOR sweep in use; (0, 0, 0) for the per-subroutine path."""
+        out = (C.c_int * 3)()
+        self._check(self.lib.les_gpu_sor_shape(self._h, out), "sor_shape")
+        return int(out[0]), int(out[1]), int(out[2])
 
     def profile(self, what: int, reps: int) -> float:
         """Average ms per repetition of one stage (it really runs and advances the state)."""

@@ -54,6 +54,20 @@ def test_batch_member_same_alone_and_in_mix(built_lib):
     b.close()
 
 
+def test_batch_member_switches_to_narrow_sor_tiles(built_lib):
+    """A 150-wide domain alone uses 32-column SOR tiles; as a batch member (the GPU
+    shared) it moves to 16-column tiles, which waste fewer ring and padding columns,
+    and marches k whole."""
+    sc = scenario(150, 150, 8, seed=84)
+    d = make_gpu(sc, lesgpu.Params(nmaxp=2))
+    assert d.sor_shape()[0] == 32
+    b = lesgpu.Batch()
+    b.add(d, 1, 1)
+    nx, ny, kchunk = d.sor_shape()
+    assert nx == 16 and kchunk == sc.km
+    b.close()
+
+
 def test_batch_members_vs_fp64_oracle(built_lib):
     """Ensemble members with their own seed, inflow direction and speed: each within
     the 1e-4 contract of the FP64 oracle after 8 steps."""

@@ -101,6 +101,41 @@ def test_sor_k_chunks_match_one_chunk(built_lib, monkeypatch, kchunk):
     assert abs(da["sor"] - db["sor"]) <= 1e-6 * abs(da["sor"])
 
 
+@pytest.mark.parametrize("shape", [(16, 16, 0), (16, 20, 0), (16, 24, 0), (16, 28, 0), (32, 20, 0), (32, 28, 5)])
+def test_sor_tile_shapes_match(built_lib, shape):
+    """Every tile shape of the fused SOR sweep -- 16- and 32-column tiles, each tile
+    height, k chunks -- gives the same fields bit for bit.  130 cells wide: three
+    16-column tiles (the last one partial) against two 32-column ones."""
+    sc = scenario(130, 36, 14, seed=73)
+    params = lesgpu.Params(nmaxp=9)
+
+    def run(nx, ny, kchunk):
+        d = make_gpu(sc, params)
+        d.set_sor_shape(nx, ny, kchunk)
+        for n in range(1, 5):
+            d.step(n, 4)
+        d.sync()
+        return d
+
+    a, b = run(32, 24, 1000), run(*shape)
+    assert a.sor_shape() == (32, 24, 14)
+    nx, ny, kchunk = shape
+    assert b.sor_shape() == (nx, ny, kchunk if (kchunk and nx == 32) else 14)
+    for fid in lesgpu.STATE_FIELDS:
+        x, y = a.download(fid), b.download(fid)
+        assert np.array_equal(x.view(np.uint32), y.view(np.uint32)), (shape, lesgpu.FIELD_NAMES[fid])
+    da, db = a.diag(), b.diag()
+    assert da["iters"] == db["iters"] == 9
+    assert abs(da["sor"] - db["sor"]) <= 1e-6 * abs(da["sor"])
+
+
+def test_sor_shape_rejects_unbuilt_shapes(built_lib):
+    d = lesgpu.Domain(40, 20, 8, lesgpu.Params())
+    for bad in ((8, 24, 0), (32, 32, 0), (32, 24, -1)):
+        with pytest.raises(lesgpu.LesError):
+            d.set_sor_shape(*bad)
+
+
 @pytest.mark.parametrize("spacing", [(4.0, 4.0), (3.0, 5.0)])
 def test_step_reciprocal_division_matches_ieee(built_lib, monkeypatch, spacing):
     """The reciprocal-corrected divisions (and the power-of-two multiplications) give
