@@ -232,6 +232,8 @@ def ensemble(specs, warmup, steps, params=None):
         d = lesgpu.Domain(sc.im, sc.jm, sc.km, params)
         d.setup_scenario(sc)
         doms.append(d)
+    # SOR tile shape per size class, measured with the GPU shared (before any timing)
+    lesgpu.tune_classes(doms, shared=True)
     b = lesgpu.Batch()
     for d in doms:
         b.add(d, 1, 10**6)
@@ -255,6 +257,7 @@ def one_by_one(specs, warmup, steps, params=None):
     for sc in specs:
         d = lesgpu.Domain(sc.im, sc.jm, sc.km, params)
         d.setup_scenario(sc)
+        lesgpu.tune_classes([d], shared=False)  # the plain path's SOR shape, measured alone
         for n in range(1, warmup + 1):
             d.step(n, 10**6)
         d.sync()
@@ -317,6 +320,7 @@ def run_ours(args):
     cells = IM * JM * KM
     dom = lesgpu.Domain(IM, JM, KM, lesgpu.Params())
     dom.setup_scenario(scenario(seed=1 + rank, im=IM, jm=JM, km=KM))
+    sor_shape, sor_tuned_us, _ = dom.tune_sor(False)  # measured SOR tile shape (untimed set-up)
     stream = torch.cuda.ExternalStream(dom.stream())
     nmax = args.warmup + args.steps + 10**6
     n = 1
@@ -383,6 +387,8 @@ def run_ours(args):
                 "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                 "traffic": (tpc * cells) if tpc else None, "ms_per_launch": sor_ms,
                 "alg_bytes_per_launch": alg,
+                "sor_tile": {"nx": sor_shape[0], "ny": sor_shape[1], "kchunk": sor_shape[2],
+                             "tuner_us": sor_tuned_us},
                 "step_alg_GBps": BYTES_PER_CELL_STEP * cells / (ms / args.steps / 1e3) / 1e9,
                 "step_frac": BYTES_PER_CELL_STEP * cells / (ms / args.steps / 1e3) / 1e9 / peak}
     dom.close()

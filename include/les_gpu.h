@@ -236,6 +236,22 @@ int les_batch_last_error(les_batch *b, char *buf, size_t len);
 int les_gpu_set_sor_shape(les_handle *h, int nx, int ny, int kchunk);
 int les_gpu_sor_shape(les_handle *h, int out[3]);
 
+/* Autotuner of the SOR tile shape per size class (im, jm, km, and the device).  It
+ * times the candidate shapes on scratch copies of this domain's SOR buffers: with
+ * shared = 0 the domain alone on the GPU (tile heights x k chunks), with shared = 1
+ * many replicas running at once, the way batch members share the GPU (16- and
+ * 32-column tiles).  The fastest shape goes into a process-wide table that domains
+ * of the class use from their next step on (les_batch_add marks a member shared);
+ * les_gpu_set_sor_shape still overrides it.  Run it while nothing else uses the GPU.
+ * out (or NULL): the shape chosen, {0,0,0} when the domain has no fused sweep;
+ * us (or NULL): its microseconds per SOR iteration and domain; report (or NULL): the
+ * candidates' timings as text, truncated to len bytes.
+ * les_sor_tuned reads the table (1: found, 0: not tuned); les_sor_set_tuned writes an
+ * entry (e.g. from a saved table), nx = 0 erases it. */
+int les_gpu_tune_sor(les_handle *h, int shared, int out[3], double *us, char *report, size_t len);
+int les_sor_tuned(int im, int jm, int km, int shared, int device, int out[3]);
+int les_sor_set_tuned(int im, int jm, int km, int shared, int device, int nx, int ny, int kchunk);
+
 /* Profiling: queue `reps` back-to-back launches of one stage on the handle's stream,
  * bracketed by CUDA events, and return the average milliseconds per repetition.
  * The stage really runs (it advances the state).  what: LES_PROF_*. */

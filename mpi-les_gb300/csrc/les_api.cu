@@ -18,6 +18,7 @@
 #include "les_common.cuh"
 #include "les_kernels.cuh"
 #include "les_step.cuh"
+#include "les_tune.cuh"
 
 namespace {
 
@@ -742,6 +743,68 @@ extern "C" int les_gpu_sor_shape(les_handle *h, int out[3]) {
   out[0] = sh.ny > 0 ? sh.nx : 0;
   out[1] = sh.ny;
   out[2] = sh.ny > 0 ? sh.kchunk : 0;
+  return LES_OK;
+}
+
+extern "C" int les_gpu_tune_sor(les_handle *h, int shared, int out[3], double *us, char *report, size_t len) {
+  NEED_COMMIT(h);
+  CK(h, cudaSetDevice(h->dev));
+  CK(h, cudaStreamSynchronize(h->s));
+  size_t free_b = 0, total_b = 0;
+  CK(h, cudaMemGetInfo(&free_b, &total_b));
+  const size_t budget = std::min<size_t>((size_t)4 << 30, free_b / 4);
+  LesDom d = h->dom;
+  d.sor_ksplit = shared ? 1 : 0;
+  SorShape best;
+  double sec = 0.0;
+  std::string rep;
+  const int rc = les_tune_sor(d, shared != 0, budget, &best, &sec, &rep);
+  if (report && len > 0) {
+    const size_t n = std::min(len - 1, rep.size());
+    memcpy(report, rep.data(), n);
+    report[n] = 0;
+  }
+  if (rc == 1) {  // odd jm or km too large: the per-subroutine SOR has no shape
+    if (out) out[0] = out[1] = out[2] = 0;
+    if (us) *us = 0.0;
+    return LES_OK;
+  }
+  if (rc != 0) return fail(h, LES_ERR_CUDA, "tune_sor: timing failed (" + std::to_string(rc) + ")");
+  if (out) {
+    out[0] = best.nx;
+    out[1] = best.ny;
+    out[2] = best.kchunk;
+  }
+  if (us) *us = sec * 1e6;
+  les_step_plan_free(&h->plan);  // re-plan with the tuned shape at the next step
+  return LES_OK;
+}
+
+extern "C" int les_sor_tuned(int im, int jm, int km, int shared, int device, int out[3]) {
+  if (!out) return LES_ERR_ARG;
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return LES_ERR_CUDA;
+  }
+  SorShape sh;
+  if (!les_tune_lookup(im, jm, km, shared, sms, &sh)) return 0;
+  out[0] = sh.nx;
+  out[1] = sh.ny;
+  out[2] = sh.kchunk;
+  return 1;
+}
+
+extern "C" int les_sor_set_tuned(int im, int jm, int km, int shared, int device, int nx, int ny, int kchunk) {
+  if (im < 1 || jm < 1 || km < 1 || (nx != 0 && nx != 16 && nx != 32) ||
+      (nx != 0 && ny != 16 && ny != 20 && ny != 24 && ny != 28) || kchunk < 0)
+    return LES_ERR_ARG;
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return LES_ERR_CUDA;
+  }
+  les_tune_store(im, jm, km, shared, sms, SorShape{nx, ny, kchunk > 0 ? std::min(kchunk, km) : km});
   return LES_OK;
 }
 

@@ -13,6 +13,7 @@
 
 #include "les_sor.cuh"
 #include "les_step.cuh"
+#include "les_tune.cuh"
 
 int les_step_parts_needed(int im, int jm, int km, int sms) {
   int worst = 0;
@@ -40,7 +41,10 @@ void les_step_plan_free(LesStepPlan *plan) {
 SorShape les_step_pick_shape(const LesDom &d) {
   if (d.jm % 2 != 0) return SorShape{};            // the wrapped j ring needs an even jm
   if (d.km + 1 >= LES_SOR_KMAX) return SorShape{};  // per-k coefficients staged in shared memory
-  SorShape sh = les_sor_pick_shape(d.im, d.jm, d.sms > 0 ? d.sms : 152, d.sor_ksplit != 0);
+  const int sms = d.sms > 0 ? d.sms : 152;
+  SorShape sh;
+  // a measured shape for the size class (les_tune_sor), else the model's choice
+  if (!les_tune_lookup(d.im, d.jm, d.km, d.sor_ksplit != 0, sms, &sh)) sh = les_sor_pick_shape(d.im, d.jm, sms, d.sor_ksplit != 0);
   // A/B measurements: LES_SOR_NX (32, 16), LES_SOR_NY (16, 20, 24, 28)
   if (const char *e = getenv("LES_SOR_NX")) {
     const int v = atoi(e);
@@ -64,6 +68,7 @@ static void plan_pick(const LesDom &d, LesStepPlan *plan) {
     // 16-column tiles march the whole k range (no k-chunk kernels are built for them)
     int kc = d.km;
     if (sh.nx == 32 && plan->fixed.kchunk > 0) kc = plan->fixed.kchunk;
+    else if (sh.nx == 32 && sh.kchunk > 0 && !plan->fixed.nx && !plan->fixed.ny) kc = sh.kchunk;  // tuned
     else if (sh.nx == 32 && !d.sor_ksplit) kc = les_sor_pick_kchunk(tiles, d.km, d.sms > 0 ? d.sms : 152);
     kc = kc < 1 ? 1 : (kc > d.km ? d.km : kc);
     if (plan->part_cap > 0 && (long long)tiles * ((d.km + kc - 1) / kc) > plan->part_cap) kc = d.km;

@@ -182,6 +182,10 @@ def load_library(path: str | None = None) -> C.CDLL:
         "les_gpu_profile": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(C.c_double)]),
         "les_gpu_set_sor_shape": (C.c_int, [vp, C.c_int, C.c_int, C.c_int]),
         "les_gpu_sor_shape": (C.c_int, [vp, C.POINTER(C.c_int)]),
+        "les_gpu_tune_sor": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double), C.c_char_p,
+                                       C.c_size_t]),
+        "les_sor_tuned": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int)]),
+        "les_sor_set_tuned": (C.c_int, [C.c_int] * 8),
         "les_batch_create": (C.c_int, [C.POINTER(vp)]),
         "les_batch_destroy": (C.c_int, [vp]),
         "les_batch_admit": (C.c_int, [C.POINTER(LesDims), C.c_size_t, ip_]),
@@ -235,6 +239,36 @@ def generate_scenario(sc: Scenario):
 
 class LesError(RuntimeError):
     pass
+
+
+def sor_tuned(im: int, jm: int, km: int, shared: bool, device: int = 0):
+    """The tuned SOR shape (nx, ny, kchunk) of a size class, or None if it was never tuned."""
+    out = (C.c_int * 3)()
+    rc = load_library().les_sor_tuned(im, jm, km, 1 if shared else 0, device, out)
+    if rc < 0:
+        raise LesError(f"les_sor_tuned: {ERRORS.get(rc, rc)}")
+    return (int(out[0]), int(out[1]), int(out[2])) if rc == 1 else None
+
+
+def set_sor_tuned(im: int, jm: int, km: int, shared: bool, shape, device: int = 0) -> None:
+    """Enter (or with shape None erase) a size class's SOR shape in the tuned table."""
+    nx, ny, kc = shape if shape else (0, 0, 0)
+    rc = load_library().les_sor_set_tuned(im, jm, km, 1 if shared else 0, device, nx, ny, kc)
+    if rc:
+        raise LesError(f"les_sor_set_tuned: {ERRORS.get(rc, rc)}")
+
+
+def tune_classes(domains, shared: bool) -> dict:
+    """Tune the SOR shape once per size class among `domains` (committed Domain
+    objects) that has no tuned entry yet; returns {(im, jm, km): (shape, us)}."""
+    done = {}
+    for d in domains:
+        key = (d.im, d.jm, d.km)
+        if key in done or sor_tuned(*key, shared) is not None:
+            continue
+        shape, us, _ = d.tune_sor(shared)
+        done[key] = (shape, us)
+    return done
 
 
 class Domain:
@@ -368,6 +402,16 @@ class Domain:
         out = (C.c_int * 3)()
         self._check(self.lib.les_gpu_sor_shape(self._h, out), "sor_shape")
         return int(out[0]), int(out[1]), int(out[2])
+
+    def tune_sor(self, shared: bool) -> tuple[tuple[int, int, int], float, str]:
+        """Time the SOR tile shapes for this domain's size class (alone, or sharing the
+        GPU with other domains), keep the fastest for the class; returns (shape,
+        microseconds per iteration, report of every candidate)."""
+        out = (C.c_int * 3)()
+        us = C.c_double(0.0)
+        rep = C.create_string_buffer(8192)
+        self._check(self.lib.les_gpu_tune_sor(self._h, 1 if shared else 0, out, C.byref(us), rep, 8192), "tune_sor")
+        return (int(out[0]), int(out[1]), int(out[2])), us.value, rep.value.decode()
 
     def profile(self, what: int, reps: int) -> float:
         """Average ms per repetition of one stage (it really runs and advances the state)."""
