@@ -16,11 +16,11 @@ void launch16(const LesDom &d, const SorArgs &a, const CUtensorMap *tp, const CU
 
 void les_launch_sor_iter_nx16(const LesDom &d, const SorArgs &a, int ny, const CUtensorMap *tp,
                               const CUtensorMap *tr, cudaStream_t s) {
-  // shared memory per CTA stays below half an SM's: D * NY * 512 + NY * 512 + 6 KB
+  // shared memory per CTA stays below half an SM's: (2 D + 2) * NY * 256 B + 6 KB
   switch (ny) {
     case 16: launch16<16, 6>(d, a, tp, tr, s); break;
     case 20: launch16<20, 6>(d, a, tp, tr, s); break;
-    case 28: launch16<28, 6>(d, a, tp, tr, s); break;
+    case 28: launch16<28, 4>(d, a, tp, tr, s); break;
     default: launch16<24, 6>(d, a, tp, tr, s); break;
   }
 }

@@ -86,7 +86,10 @@ template <int NX>
 __device__ __forceinline__ Lane make_lane(const LesDom &d, int tj, int ny) {
   Lane L;
   L.c4 = threadIdx.x;
-  L.r = threadIdx.y;
+  // 16-column tiles: a warp holds two rows two apart (rows 0,2 | 1,3 | 4,6 | 5,7 ...), so
+  // both rows have the same red/black parity and the colour branch stays warp-uniform
+  L.r = (NX == 16) ? 4 * ((int)threadIdx.y >> 2) + (((int)threadIdx.y >> 1) & 1) + 2 * ((int)threadIdx.y & 1)
+                   : (int)threadIdx.y;
   const int i0 = 1 + blockIdx.x * tile_i(NX);
   const int j0 = 1 + blockIdx.y * tj;
   L.ib = i0 - 4 + 4 * L.c4;
