@@ -141,7 +141,7 @@ extern "C" size_t les_domain_bytes(int im, int jm, int km) {
   const size_t field = pi * nj * nk * sizeof(float);
   const size_t part = ((size_t)(im + 63) / 64 + 1) * ((size_t)(jm + 3) / 4 + 1) * (size_t)km * 2 * sizeof(double);
   // deferred-block lists (les_gpu_create): FIX_COUNT lists over the largest grid of those kernels
-  const size_t fused = (size_t)((im + 31) / 32) * ((jm + 1) / 2) * ((km + 3) / 4);
+  const size_t fused = (size_t)((im + 30) / 31) * ((jm + 7) / 8) * km;  // velfg k-march: tile planes
   const size_t inter = (size_t)((im + 63) / 64) * ((jm + 3) / 4) * km;
   const size_t march = (size_t)((im + 31) / 32) * ((jm + 7) / 8) * km;
   const size_t fix = FIX_COUNT * (2 + std::max({fused, inter, march})) * sizeof(int);
@@ -217,7 +217,7 @@ extern "C" int les_gpu_create(const les_dims *dims, const les_params *params, le
   h->plan.part_cap = (long long)h->npart;
   // deferred-block lists: [count, ticket, ids...] for the largest grid of those kernels
   {
-    const long long fused = (long long)((im + 31) / 32) * ((jm + 1) / 2) * ((km + 3) / 4);
+    const long long fused = (long long)((im + 30) / 31) * ((jm + 7) / 8) * km;  // velfg k-march: tile planes
     const long long inter = (long long)((im + 63) / 64) * ((jm + 3) / 4) * km;
     const long long march = (long long)((im + 31) / 32) * ((jm + 7) / 8) * km;  // les k-march: tile planes
     h->fix_len = 2 + (size_t)std::max({fused, inter, march});

@@ -21,6 +21,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 
 #include "les_common.cuh"
 #include "les_kernels.cuh"
@@ -49,86 +50,105 @@ struct NouDiu {
 };
 
 // ---- the nine face pairs of vel2.f95:74-197, with the halo copies of :202-318 as
-// index remaps.  P2 / ZF select the division forms (dvs, dvz); bd collects dividends
-// outside the reciprocal-corrected range.
+// index remaps.  Each face is split into its loads (fload<N>: the velocities it reads)
+// and its arithmetic (fcomp<N>), so a kernel can issue the loads of one plane while it
+// computes another; faceN = fcomp<N>(fload<N>).  P2 / ZF select the division forms
+// (dvs, dvz); bd collects dividends outside the reciprocal-corrected range.
+struct FRaw {
+  float a = 0.f, b = 0.f, c = 0.f, e = 0.f;
+};
+
+template <int N>
+__device__ __forceinline__ FRaw fload(const LesDom &d, int i, int j, int k) {
+  FRaw r;
+  const int ii = min(i, d.im), jj = (j > d.jm) ? 1 : j;
+  if (N == 1) { r.a = UR_(ii - 1, j, k); r.b = UR_(ii, j, k); }
+  if (N == 2) { r.a = VR_(i, jj - 1, k); r.b = VR_(i + 1, jj - 1, k); r.c = UR_(i, jj - 1, k); r.e = UR_(i, jj, k); }
+  if (N == 3) {
+    if (k == 1) { r.a = WR_(i, j, 1); r.b = WR_(i + 1, j, 1); r.c = DIU_(3, i, j, 1); }
+    else { r.a = WR_(i, j, k - 1); r.b = WR_(i + 1, j, k - 1); r.c = UR_(i, j, k - 1); r.e = UR_(i, j, k); }
+  }
+  if (N == 4) { r.a = UR_(ii - 1, j, k); r.b = UR_(ii - 1, j + 1, k); r.c = VR_(ii - 1, j, k); r.e = VR_(ii, j, k); }
+  if (N == 5) { r.a = VR_(i, jj - 1, k); r.b = VR_(i, jj, k); }
+  if (N == 6) {
+    if (k == 1) { r.a = WR_(i, j, 1); r.b = WR_(i, j + 1, 1); r.c = DIU_(6, i, j, 1); }
+    else { r.a = WR_(i, j, k - 1); r.b = WR_(i, j + 1, k - 1); r.c = VR_(i, j, k - 1); r.e = VR_(i, j, k); }
+  }
+  if (N == 7) { r.a = UR_(ii - 1, j, k); r.b = UR_(ii - 1, j, k + 1); r.c = WR_(ii - 1, j, k); r.e = WR_(ii, j, k); }
+  if (N == 8) { r.a = VR_(i, jj - 1, k); r.b = VR_(i, jj - 1, k + 1); r.c = WR_(i, jj - 1, k); r.e = WR_(i, jj, k); }
+  if (N == 9) { r.a = WR_(i, j, k - 1); r.b = WR_(i, j, k); }
+  return r;
+}
+
+// diu3 and diu6 at k = 1 are the log-law wall gradients, stored by k_wall before velfg runs
+template <int N, bool P2, bool ZF>
+__device__ __forceinline__ NouDiu fcomp(const LesDom &d, const FRaw &r, int i, int j, int k, unsigned &bd) {
+  const float *dx1 = d.gr.dx1, *dy1 = d.gr.dy1, *dzn = d.gr.dzn;
+  const int ii = min(i, d.im), jj = (j > d.jm) ? 1 : j;
+  if (N == 1) return {(r.a + r.b) / 2.f, dvs<P2, ZF>(-r.a + r.b, dx1[ii], d.gr.rdx1[ii], bd)};
+  if (N == 2)
+    return {dvs<P2, ZF>(dx1[i + 1] * r.a + dx1[i] * r.b, dx1[i] + dx1[i + 1], d.gr.rdx1s[i], bd),
+            dvs<P2, ZF>(2.f * (-r.c + r.e), dy1[jj - 1] + dy1[jj], d.gr.rdy1s[jj - 1], bd)};
+  if (N == 3) {
+    if (k == 1)
+      return {dvs<P2, ZF>(0.5f * (dx1[i + 1] * r.a + dx1[i] * r.b), dx1[i] + dx1[i + 1], d.gr.rdx1s[i], bd), r.c};
+    return {dvs<P2, ZF>(dx1[i + 1] * r.a + dx1[i] * r.b, dx1[i] + dx1[i + 1], d.gr.rdx1s[i], bd),
+            dvz<ZF>(-r.c + r.e, d.gr.dzs[k - 1], d.gr.rdzs[k - 1], bd)};
+  }
+  if (N == 4)
+    return {dvs<P2, ZF>(dy1[j + 1] * r.a + dy1[j] * r.b, dy1[j] + dy1[j + 1], d.gr.rdy1s[j], bd) - 0.f,
+            dvs<P2, ZF>(2.f * (-r.c + r.e), dx1[ii - 1] + dx1[ii], d.gr.rdx1s[ii - 1], bd)};
+  if (N == 5) return {(r.a + r.b) / 2.f, dvs<P2, ZF>(-r.a + r.b, dy1[jj], d.gr.rdy1[jj], bd)};
+  if (N == 6) {
+    if (k == 1)
+      return {dvs<P2, ZF>(0.5f * (dy1[j + 1] * r.a + dy1[j] * r.b), dy1[j] + dy1[j + 1], d.gr.rdy1s[j], bd), r.c};
+    return {dvs<P2, ZF>(dy1[j + 1] * r.a + dy1[j] * r.b, dy1[j] + dy1[j + 1], d.gr.rdy1s[j], bd),
+            dvz<ZF>(-r.c + r.e, d.gr.dzs[k - 1], d.gr.rdzs[k - 1], bd)};
+  }
+  if (N == 7)
+    return {dvz<ZF>(dzn[k + 1] * r.a + dzn[k] * r.b, dzn[k] + dzn[k + 1], d.gr.rdzsum[k], bd) - 0.f,
+            dvs<P2, ZF>(2.f * (-r.c + r.e), dx1[ii - 1] + dx1[ii], d.gr.rdx1s[ii - 1], bd)};
+  if (N == 8)
+    return {dvz<ZF>(dzn[k + 1] * r.a + dzn[k] * r.b, dzn[k] + dzn[k + 1], d.gr.rdzsum[k], bd),
+            dvs<P2, ZF>(2.f * (-r.c + r.e), dy1[jj - 1] + dy1[jj], d.gr.rdy1s[jj - 1], bd)};
+  return {(r.a + r.b) / 2.f, dvz<ZF>(-r.a + r.b, dzn[k], d.gr.rdzn[k], bd)};  // N == 9
+}
+
 template <bool P2, bool ZF>
 __device__ __forceinline__ NouDiu face1(const LesDom &d, int i, int j, int k, unsigned &bd) {
-  const int ii = min(i, d.im);
-  const float a = UR_(ii - 1, j, k), b = UR_(ii, j, k);
-  return {(a + b) / 2.f, dvs<P2, ZF>(-a + b, d.gr.dx1[ii], d.gr.rdx1[ii], bd)};
+  return fcomp<1, P2, ZF>(d, fload<1>(d, i, j, k), i, j, k, bd);
 }
 template <bool P2, bool ZF>
 __device__ __forceinline__ NouDiu face2(const LesDom &d, int i, int j, int k, unsigned &bd) {
-  const int jj = (j > d.jm) ? 1 : j;
-  const float *dx1 = d.gr.dx1, *dy1 = d.gr.dy1;
-  const float nou = dvs<P2, ZF>(dx1[i + 1] * VR_(i, jj - 1, k) + dx1[i] * VR_(i + 1, jj - 1, k), dx1[i] + dx1[i + 1],
-                                d.gr.rdx1s[i], bd);
-  const float diu = dvs<P2, ZF>(2.f * (-UR_(i, jj - 1, k) + UR_(i, jj, k)), dy1[jj - 1] + dy1[jj], d.gr.rdy1s[jj - 1], bd);
-  return {nou, diu};
+  return fcomp<2, P2, ZF>(d, fload<2>(d, i, j, k), i, j, k, bd);
 }
-// diu3 at k = 1 is the log-law wall gradient, stored by k_wall before this kernel runs
 template <bool P2, bool ZF>
 __device__ __forceinline__ NouDiu face3(const LesDom &d, int i, int j, int k, unsigned &bd) {
-  const float *dx1 = d.gr.dx1;
-  if (k == 1) {
-    const float nou = dvs<P2, ZF>(0.5f * (dx1[i + 1] * WR_(i, j, 1) + dx1[i] * WR_(i + 1, j, 1)), dx1[i] + dx1[i + 1],
-                                  d.gr.rdx1s[i], bd);
-    return {nou, DIU_(3, i, j, 1)};
-  }
-  const float nou = dvs<P2, ZF>(dx1[i + 1] * WR_(i, j, k - 1) + dx1[i] * WR_(i + 1, j, k - 1), dx1[i] + dx1[i + 1],
-                                d.gr.rdx1s[i], bd);
-  return {nou, dvz<ZF>(-UR_(i, j, k - 1) + UR_(i, j, k), d.gr.dzs[k - 1], d.gr.rdzs[k - 1], bd)};
+  return fcomp<3, P2, ZF>(d, fload<3>(d, i, j, k), i, j, k, bd);
 }
 template <bool P2, bool ZF>
 __device__ __forceinline__ NouDiu face4(const LesDom &d, int i, int j, int k, unsigned &bd) {
-  const int ii = min(i, d.im);
-  const float *dx1 = d.gr.dx1, *dy1 = d.gr.dy1;
-  const float nou = dvs<P2, ZF>(dy1[j + 1] * UR_(ii - 1, j, k) + dy1[j] * UR_(ii - 1, j + 1, k), dy1[j] + dy1[j + 1],
-                                d.gr.rdy1s[j], bd);
-  const float diu = dvs<P2, ZF>(2.f * (-VR_(ii - 1, j, k) + VR_(ii, j, k)), dx1[ii - 1] + dx1[ii], d.gr.rdx1s[ii - 1], bd);
-  return {nou - 0.f, diu};
+  return fcomp<4, P2, ZF>(d, fload<4>(d, i, j, k), i, j, k, bd);
 }
 template <bool P2, bool ZF>
 __device__ __forceinline__ NouDiu face5(const LesDom &d, int i, int j, int k, unsigned &bd) {
-  const int jj = (j > d.jm) ? 1 : j;
-  const float a = VR_(i, jj - 1, k), b = VR_(i, jj, k);
-  return {(a + b) / 2.f, dvs<P2, ZF>(-a + b, d.gr.dy1[jj], d.gr.rdy1[jj], bd)};
+  return fcomp<5, P2, ZF>(d, fload<5>(d, i, j, k), i, j, k, bd);
 }
-// diu6 at k = 1: stored by k_wall
 template <bool P2, bool ZF>
 __device__ __forceinline__ NouDiu face6(const LesDom &d, int i, int j, int k, unsigned &bd) {
-  const float *dy1 = d.gr.dy1;
-  if (k == 1) {
-    const float nou = dvs<P2, ZF>(0.5f * (dy1[j + 1] * WR_(i, j, 1) + dy1[j] * WR_(i, j + 1, 1)), dy1[j] + dy1[j + 1],
-                                  d.gr.rdy1s[j], bd);
-    return {nou, DIU_(6, i, j, 1)};
-  }
-  const float nou = dvs<P2, ZF>(dy1[j + 1] * WR_(i, j, k - 1) + dy1[j] * WR_(i, j + 1, k - 1), dy1[j] + dy1[j + 1],
-                                d.gr.rdy1s[j], bd);
-  return {nou, dvz<ZF>(-VR_(i, j, k - 1) + VR_(i, j, k), d.gr.dzs[k - 1], d.gr.rdzs[k - 1], bd)};
+  return fcomp<6, P2, ZF>(d, fload<6>(d, i, j, k), i, j, k, bd);
 }
 template <bool P2, bool ZF>
 __device__ __forceinline__ NouDiu face7(const LesDom &d, int i, int j, int k, unsigned &bd) {
-  const int ii = min(i, d.im);
-  const float *dx1 = d.gr.dx1, *dzn = d.gr.dzn;
-  const float nou =
-      dvz<ZF>(dzn[k + 1] * UR_(ii - 1, j, k) + dzn[k] * UR_(ii - 1, j, k + 1), dzn[k] + dzn[k + 1], d.gr.rdzsum[k], bd);
-  const float diu = dvs<P2, ZF>(2.f * (-WR_(ii - 1, j, k) + WR_(ii, j, k)), dx1[ii - 1] + dx1[ii], d.gr.rdx1s[ii - 1], bd);
-  return {nou - 0.f, diu};
+  return fcomp<7, P2, ZF>(d, fload<7>(d, i, j, k), i, j, k, bd);
 }
 template <bool P2, bool ZF>
 __device__ __forceinline__ NouDiu face8(const LesDom &d, int i, int j, int k, unsigned &bd) {
-  const int jj = (j > d.jm) ? 1 : j;
-  const float *dy1 = d.gr.dy1, *dzn = d.gr.dzn;
-  const float nou =
-      dvz<ZF>(dzn[k + 1] * VR_(i, jj - 1, k) + dzn[k] * VR_(i, jj - 1, k + 1), dzn[k] + dzn[k + 1], d.gr.rdzsum[k], bd);
-  const float diu = dvs<P2, ZF>(2.f * (-WR_(i, jj - 1, k) + WR_(i, jj, k)), dy1[jj - 1] + dy1[jj], d.gr.rdy1s[jj - 1], bd);
-  return {nou, diu};
+  return fcomp<8, P2, ZF>(d, fload<8>(d, i, j, k), i, j, k, bd);
 }
 template <bool ZF>
 __device__ __forceinline__ NouDiu face9(const LesDom &d, int i, int j, int k, unsigned &bd) {
-  const float a = WR_(i, j, k - 1), b = WR_(i, j, k);
-  return {(a + b) / 2.f, dvz<ZF>(-a + b, d.gr.dzn[k], d.gr.rdzn[k], bd)};
+  return fcomp<9, false, ZF>(d, fload<9>(d, i, j, k), i, j, k, bd);
 }
 
 // ------------------------------------------------------------------ vel2.f95:54-65,138,173,351-356
@@ -155,50 +175,76 @@ struct VelfgOut {
   float d1, d2, d3, d4, d5, d6, d7, d8, d9;
   float d3t, d6t;  // diu3, diu6 at km+1 (k = km only)
 };
+// The momentum terms of one cell from its six face pairs per component: a, b at i and
+// i+1, y0, y1 at j and j+1, z0, z1 at k and k+1 (velFG.f95:64-110).
+template <bool P2, bool ZF>
+__device__ __forceinline__ float velfg_fu(const LesDom &d, int i, int j, int k, const NouDiu &a, const NouDiu &b,
+                                          const NouDiu &y0, const NouDiu &y1, const NouDiu &z0, const NouDiu &z1,
+                                          unsigned &bd) {
+  const float *dx1 = d.gr.dx1;
+  const float covx1 =
+      dvs<P2, ZF>(dx1[i + 1] * (a.nou * a.diu) + dx1[i] * (b.nou * b.diu), dx1[i] + dx1[i + 1], d.gr.rdx1s[i], bd);
+  const float covy1 = (y0.nou * y0.diu + y1.nou * y1.diu) / 2.f;
+  const float covz1 = (z0.nou * z0.diu + z1.nou * z1.diu) / 2.f;
+  const float covc = covx1 + covy1 + covz1;
+  const float dfu1 = dvs<P2, ZF>(2.f * (-a.diu + b.diu), dx1[i] + dx1[i + 1], d.gr.rdx1s[i], bd) +
+                     dvs<P2, ZF>(-y0.diu + y1.diu, d.gr.dy1[j], d.gr.rdy1[j], bd) +
+                     dvz<ZF>(-z0.diu + z1.diu, d.gr.dzn[k], d.gr.rdzn[k], bd);
+  return (-covc + d.vn * dfu1);
+}
+template <bool P2, bool ZF>
+__device__ __forceinline__ float velfg_fv(const LesDom &d, int i, int j, int k, const NouDiu &a, const NouDiu &b,
+                                          const NouDiu &y0, const NouDiu &y1, const NouDiu &z0, const NouDiu &z1,
+                                          unsigned &bd) {
+  const float *dy1 = d.gr.dy1;
+  const float covx1 = (a.nou * a.diu + b.nou * b.diu) / 2.f;
+  const float covy1 =
+      dvs<P2, ZF>(dy1[j + 1] * (y0.nou * y0.diu) + dy1[j] * (y1.nou * y1.diu), dy1[j] + dy1[j + 1], d.gr.rdy1s[j], bd);
+  const float covz1 = (z0.nou * z0.diu + z1.nou * z1.diu) / 2.f;
+  const float covc = covx1 + covy1 + covz1;
+  const float dfv1 = dvs<P2, ZF>(-a.diu + b.diu, d.gr.dx1[i], d.gr.rdx1[i], bd) +
+                     dvs<P2, ZF>(2.f * (-y0.diu + y1.diu), dy1[j] + dy1[j + 1], d.gr.rdy1s[j], bd) +
+                     dvz<ZF>(-z0.diu + z1.diu, d.gr.dzn[k], d.gr.rdzn[k], bd);
+  return (-covc + d.vn * dfv1);
+}
+template <bool P2, bool ZF>
+__device__ __forceinline__ float velfg_fw(const LesDom &d, int i, int j, int k, const NouDiu &a, const NouDiu &b,
+                                          const NouDiu &y0, const NouDiu &y1, const NouDiu &z0, const NouDiu &z1,
+                                          unsigned &bd) {
+  const float *dzn = d.gr.dzn;
+  const float covx1 = (a.nou * a.diu + b.nou * b.diu) / 2.f;
+  const float covy1 = (y0.nou * y0.diu + y1.nou * y1.diu) / 2.f;
+  const float covz1 =
+      dvz<ZF>(dzn[k + 1] * (z0.nou * z0.diu) + dzn[k] * (z1.nou * z1.diu), dzn[k] + dzn[k + 1], d.gr.rdzsum[k], bd);
+  const float covc = covx1 + covy1 + covz1;
+  const float dfw1 = dvs<P2, ZF>(-a.diu + b.diu, d.gr.dx1[i], d.gr.rdx1[i], bd) +
+                     dvs<P2, ZF>(-y0.diu + y1.diu, d.gr.dy1[j], d.gr.rdy1[j], bd) +
+                     dvz<ZF>(-z0.diu + z1.diu, d.gr.dzs[k], d.gr.rdzs[k], bd);
+  return (-covc + d.vn * dfw1);
+}
+
 template <bool P2, bool ZF>
 __device__ __forceinline__ void velfg_cell(const LesDom &d, int i, int j, int k, int c, VelfgOut &o, unsigned &bd) {
-  const float *dx1 = d.gr.dx1, *dy1 = d.gr.dy1, *dzn = d.gr.dzn, *dzs = d.gr.dzs;
-  const float *rdx1 = d.gr.rdx1, *rdx1s = d.gr.rdx1s, *rdy1 = d.gr.rdy1, *rdy1s = d.gr.rdy1s;
-  const float *rdzn = d.gr.rdzn, *rdzs = d.gr.rdzs, *rdzsum = d.gr.rdzsum;
   {  // u
     const NouDiu a = face1<P2, ZF>(d, i, j, k, bd), b = face1<P2, ZF>(d, i + 1, j, k, bd);
     const NouDiu y0 = face2<P2, ZF>(d, i, j, k, bd), y1 = face2<P2, ZF>(d, i, j + 1, k, bd);
     const NouDiu z0 = face3<P2, ZF>(d, i, j, k, bd), z1 = face3<P2, ZF>(d, i, j, k + 1, bd);
     o.d1 = a.diu; o.d2 = y0.diu; o.d3 = z0.diu; o.d3t = z1.diu;
-    const float covx1 = dvs<P2, ZF>(dx1[i + 1] * (a.nou * a.diu) + dx1[i] * (b.nou * b.diu), dx1[i] + dx1[i + 1], rdx1s[i], bd);
-    const float covy1 = (y0.nou * y0.diu + y1.nou * y1.diu) / 2.f;
-    const float covz1 = (z0.nou * z0.diu + z1.nou * z1.diu) / 2.f;
-    const float covc = covx1 + covy1 + covz1;
-    const float dfu1 = dvs<P2, ZF>(2.f * (-a.diu + b.diu), dx1[i] + dx1[i + 1], rdx1s[i], bd) +
-                       dvs<P2, ZF>(-y0.diu + y1.diu, dy1[j], rdy1[j], bd) + dvz<ZF>(-z0.diu + z1.diu, dzn[k], rdzn[k], bd);
-    o.f = (-covc + d.vn * dfu1);
+    o.f = velfg_fu<P2, ZF>(d, i, j, k, a, b, y0, y1, z0, z1, bd);
   }
   {  // v
     const NouDiu a = face4<P2, ZF>(d, i, j, k, bd), b = face4<P2, ZF>(d, i + 1, j, k, bd);
     const NouDiu y0 = face5<P2, ZF>(d, i, j, k, bd), y1 = face5<P2, ZF>(d, i, j + 1, k, bd);
     const NouDiu z0 = face6<P2, ZF>(d, i, j, k, bd), z1 = face6<P2, ZF>(d, i, j, k + 1, bd);
     o.d4 = a.diu; o.d5 = y0.diu; o.d6 = z0.diu; o.d6t = z1.diu;
-    const float covx1 = (a.nou * a.diu + b.nou * b.diu) / 2.f;
-    const float covy1 = dvs<P2, ZF>(dy1[j + 1] * (y0.nou * y0.diu) + dy1[j] * (y1.nou * y1.diu), dy1[j] + dy1[j + 1], rdy1s[j], bd);
-    const float covz1 = (z0.nou * z0.diu + z1.nou * z1.diu) / 2.f;
-    const float covc = covx1 + covy1 + covz1;
-    const float dfv1 = dvs<P2, ZF>(-a.diu + b.diu, dx1[i], rdx1[i], bd) +
-                       dvs<P2, ZF>(2.f * (-y0.diu + y1.diu), dy1[j] + dy1[j + 1], rdy1s[j], bd) +
-                       dvz<ZF>(-z0.diu + z1.diu, dzn[k], rdzn[k], bd);
-    o.g = (-covc + d.vn * dfv1);
+    o.g = velfg_fv<P2, ZF>(d, i, j, k, a, b, y0, y1, z0, z1, bd);
   }
   if (k <= d.km - 1) {  // w
     const NouDiu a = face7<P2, ZF>(d, i, j, k, bd), b = face7<P2, ZF>(d, i + 1, j, k, bd);
     const NouDiu y0 = face8<P2, ZF>(d, i, j, k, bd), y1 = face8<P2, ZF>(d, i, j + 1, k, bd);
     const NouDiu z0 = face9<ZF>(d, i, j, k, bd), z1 = face9<ZF>(d, i, j, k + 1, bd);
     o.d7 = a.diu; o.d8 = y0.diu; o.d9 = z0.diu;
-    const float covx1 = (a.nou * a.diu + b.nou * b.diu) / 2.f;
-    const float covy1 = (y0.nou * y0.diu + y1.nou * y1.diu) / 2.f;
-    const float covz1 = dvz<ZF>(dzn[k + 1] * (z0.nou * z0.diu) + dzn[k] * (z1.nou * z1.diu), dzn[k] + dzn[k + 1], rdzsum[k], bd);
-    const float covc = covx1 + covy1 + covz1;
-    const float dfw1 = dvs<P2, ZF>(-a.diu + b.diu, dx1[i], rdx1[i], bd) + dvs<P2, ZF>(-y0.diu + y1.diu, dy1[j], rdy1[j], bd) +
-                       dvz<ZF>(-z0.diu + z1.diu, dzs[k], rdzs[k], bd);
-    o.h = (-covc + d.vn * dfw1);
+    o.h = velfg_fw<P2, ZF>(d, i, j, k, a, b, y0, y1, z0, z1, bd);
   } else {  // k = km: h keeps its value; diu7, diu8 are never written there by the reference (zero)
     o.h = d.h[c];
     o.d7 = 0.f;
@@ -207,30 +253,23 @@ __device__ __forceinline__ void velfg_cell(const LesDom &d, int i, int j, int k,
   }
 }
 
-// velfg (+ feedbf.f95:35-61 when FB) of the block (bx, by, bz).  With FB the feedback
-// force is added to f, g, h for k = 1..km (h(km) keeps velfg's untouched value).
-// ZF: reciprocal-corrected divisions, blocks with a dividend outside their range
-// deferred to the fixup kernel; !ZF: IEEE divisions.
-template <bool P2, bool ZF, bool FB>
-__device__ __forceinline__ void velfg_block(const LesDom &d, int bx, int by, int bz) {
-  // threads past the domain edge compute the edge cell again (straight-line code) and store nothing
-  const int i0 = bx * FX + threadIdx.x + 1, j0 = by * FY + threadIdx.y + 1, k0 = bz * FZ + threadIdx.z + 1;
-  const bool in = (i0 <= d.im && j0 <= d.jm && k0 <= d.km);
-  const int i = min(i0, d.im), j = min(j0, d.jm), k = min(k0, d.km);
-  const int c = lix(d, i, j, k);
-  // feedbf operands loaded up front: their latency hides behind the velfg arithmetic
+// Operands of feedbf (feedbf.f95:35-61) for one cell, loaded ahead of use.
+struct FbIn {
   uint8_t m = 0;
   float u = 0.f, v = 0.f, w = 0.f, su = 0.f, sv = 0.f, sw = 0.f;
-  if (FB) {
-    m = d.mask[c];
-    u = d.u[c]; v = d.v[c]; w = d.w[c];
-    su = d.usum[c]; sv = d.vsum[c]; sw = d.wsum[c];
-  }
-  VelfgOut o;
-  unsigned bd = 0;
-  velfg_cell<P2, ZF>(d, i, j, k, c, o, bd);
-  if (ZF && defer_block(bd, d.fix[FIX_VELFG])) return;
-  if (!in) return;
+};
+__device__ __forceinline__ FbIn fb_load(const LesDom &d, int c) {
+  FbIn x;
+  x.m = d.mask[c];
+  x.u = d.u[c]; x.v = d.v[c]; x.w = d.w[c];
+  x.su = d.usum[c]; x.sv = d.vsum[c]; x.sw = d.wsum[c];
+  return x;
+}
+
+// Stores of one cell: the diu it formed, then f, g, h (+ feedbf when FB: the feedback
+// force added to f, g, h for k = 1..km; h(km) keeps velfg's untouched value).
+template <bool FB>
+__device__ __forceinline__ void velfg_store(const LesDom &d, int c, int k, const VelfgOut &o, const FbIn &x) {
   d.diu[1][c] = o.d1;
   d.diu[2][c] = o.d2;
   if (k > 1) d.diu[3][c] = o.d3;  // k = 1: the wall gradient stored by k_wall
@@ -246,28 +285,212 @@ __device__ __forceinline__ void velfg_block(const LesDom &d, int bx, int by, int
   }
   float fv = o.f, gv = o.g, hv = o.h;
   if (FB) {  // feedbf.f95:35-61
-    const float bm = (m & 1) ? 1.f : 0.f, cm = (m & 2) ? 1.f : 0.f, dm = (m & 4) ? 1.f : 0.f;
-    const float us = (su + u) * bm;
-    const float vs = (sv + v) * cm;
-    const float ws = (sw + w) * dm;
+    const float bm = (x.m & 1) ? 1.f : 0.f, cm = (x.m & 2) ? 1.f : 0.f, dm = (x.m & 4) ? 1.f : 0.f;
+    const float us = (x.su + x.u) * bm;
+    const float vs = (x.sv + x.v) * cm;
+    const float ws = (x.sw + x.w) * dm;
     d.usum[c] = us; d.vsum[c] = vs; d.wsum[c] = ws;
-    fv = fv + (d.alpha * us * d.dt + d.beta * u * bm);
-    gv = gv + (d.alpha * vs * d.dt + d.beta * v * cm);
-    hv = hv + (d.alpha * ws * d.dt + d.beta * w * dm);
+    fv = fv + (d.alpha * us * d.dt + d.beta * x.u * bm);
+    gv = gv + (d.alpha * vs * d.dt + d.beta * x.v * cm);
+    hv = hv + (d.alpha * ws * d.dt + d.beta * x.w * dm);
   }
   d.f[c] = fv;
   d.g[c] = gv;
   if (FB || k <= d.km - 1) d.h[c] = hv;
 }
 
+// ---- the velfg k-march -------------------------------------------------------------
+// A block owns MTI x MTY columns (31 cells of i per 32 lanes, 8 rows of j) and marches
+// k over a chunk of planes.  Each face pair is formed once per face, not once per cell
+// that reads it: the i faces (face1, 4, 7) by the lane of the cell on their east side
+// and passed west by warp shuffle (the 32nd lane of a row forms the face east of the
+// tile), the j faces (face2, 5, 8) by the row south of them and passed north through
+// shared memory (row 0 forms the face south of the tile), the k faces (face3, 6, 9)
+// once per plane, kept in registers for the plane above.  Step k forms the faces of
+// plane k+1 and combines those of plane k; one barrier per step orders the j faces and decides whether the plane is stored (a
+// dividend outside dvz's range anywhere in the tile plane hands the plane to the fixup
+// kernel, which recomputes it with IEEE divisions).  The rows of u, v, w a thread reads
+// are requested into L1 (prefetch.global.L1) three planes before their faces are formed.
+constexpr int MTX = 32, MTI = 31, MTY = 8;
+
+struct MFaces {  // faces of one column position: u, v, w components
+  NouDiu u, v, w;
+};
+
+// The loads of the faces a thread forms for one plane.
+struct MRaw {
+  FRaw x1, x4, x7;  // i faces at (ia, j)
+  FRaw y2, y5, y8;  // j faces at (i, j+1)
+  FRaw s2, s5, s8;  // row 0: j faces at (i, j0)
+  FRaw z3, z6, z9;  // k faces at the plane above
+};
+
 template <bool P2, bool ZF, bool FB>
-__global__ void __launch_bounds__(FX *FY *FZ) k_velfg2(LesDom d) {
-  velfg_block<P2, ZF, FB>(d, blockIdx.x, blockIdx.y, blockIdx.z);
+__global__ void __launch_bounds__(MTX *MTY, 3) k_velfg_march(LesDom d, int kchunk) {
+  // j-face pairs of rows j0 .. j0+MTY for two planes (plane parity): [.][row][lane]
+  __shared__ MFaces ys[2][MTY + 1][MTX];
+  const int lane = threadIdx.x, ty = threadIdx.y;
+  const int i0 = blockIdx.x * MTI + 1, j0 = blockIdx.y * MTY + 1;
+  const int k0 = blockIdx.z * kchunk + 1, k1 = min(k0 + kchunk - 1, d.km);
+  const int iraw = i0 + lane, jraw = j0 + ty;
+  const bool in = lane < MTI && iraw <= d.im && jraw <= d.jm;
+  // the cell's column (clamped into the domain: lanes and rows past it recompute the
+  // edge and store nothing) and the column of the i face this lane forms (i = im+1 is
+  // the face east of cell im)
+  const int i = min(iraw, d.im), j = min(jraw, d.jm), ia = min(iraw, d.im + 1);
+  const int km = d.km;
+
+  // loads of plane kk's i and j faces and of the k faces at kz (kz = kk + 1)
+  auto load = [&](int kk, int kz) {
+    MRaw r;
+    r.x1 = fload<1>(d, ia, j, kk);
+    r.x4 = fload<4>(d, ia, j, kk);
+    r.y2 = fload<2>(d, i, j + 1, kk);
+    r.y5 = fload<5>(d, i, j + 1, kk);
+    if (kk <= km - 1) {
+      r.x7 = fload<7>(d, ia, j, kk);
+      r.y8 = fload<8>(d, i, j + 1, kk);
+    }
+    if (ty == 0) {
+      r.s2 = fload<2>(d, i, j, kk);
+      r.s5 = fload<5>(d, i, j, kk);
+      if (kk <= km - 1) r.s8 = fload<8>(d, i, j, kk);
+    }
+    r.z3 = fload<3>(d, i, j, kz);
+    r.z6 = fload<6>(d, i, j, kz);
+    if (kz <= km) r.z9 = fload<9>(d, i, j, kz);
+    return r;
+  };
+  // faces of plane kk from its loads: i faces returned, j faces into shared memory, k faces at kz
+  auto form = [&](const MRaw &r, int kk, int kz, MFaces &X, MFaces &Z, unsigned &fxy, unsigned &fz) {
+    X.u = fcomp<1, P2, ZF>(d, r.x1, ia, j, kk, fxy);
+    X.v = fcomp<4, P2, ZF>(d, r.x4, ia, j, kk, fxy);
+    X.w = (kk <= km - 1) ? fcomp<7, P2, ZF>(d, r.x7, ia, j, kk, fxy) : NouDiu{0.f, 0.f};
+    MFaces Y;
+    Y.u = fcomp<2, P2, ZF>(d, r.y2, i, j + 1, kk, fxy);
+    Y.v = fcomp<5, P2, ZF>(d, r.y5, i, j + 1, kk, fxy);
+    Y.w = (kk <= km - 1) ? fcomp<8, P2, ZF>(d, r.y8, i, j + 1, kk, fxy) : NouDiu{0.f, 0.f};
+    ys[kk & 1][ty + 1][lane] = Y;
+    if (ty == 0) {
+      MFaces S;
+      S.u = fcomp<2, P2, ZF>(d, r.s2, i, j, kk, fxy);
+      S.v = fcomp<5, P2, ZF>(d, r.s5, i, j, kk, fxy);
+      S.w = (kk <= km - 1) ? fcomp<8, P2, ZF>(d, r.s8, i, j, kk, fxy) : NouDiu{0.f, 0.f};
+      ys[kk & 1][0][lane] = S;
+    }
+    Z.u = fcomp<3, P2, ZF>(d, r.z3, i, j, kz, fz);
+    Z.v = fcomp<6, P2, ZF>(d, r.z6, i, j, kz, fz);
+    Z.w = (kz <= km) ? fcomp<9, false, ZF>(d, r.z9, i, j, kz, fz) : NouDiu{0.f, 0.f};
+  };
+
+  // prologue: the faces of plane k0 and the k faces at k0, k0+1
+  unsigned fz0 = 0, fz1 = 0, fxy = 0;
+  MFaces X, Z0, Z1;
+  {
+    const MRaw r = load(k0, k0 + 1);
+    form(r, k0, k0 + 1, X, Z1, fxy, fz1);
+    Z0.u = fcomp<3, P2, ZF>(d, fload<3>(d, i, j, k0), i, j, k0, fz0);
+    Z0.v = fcomp<6, P2, ZF>(d, fload<6>(d, i, j, k0), i, j, k0, fz0);
+    Z0.w = fcomp<9, false, ZF>(d, fload<9>(d, i, j, k0), i, j, k0, fz0);
+  }
+  int c = lix(d, i, j, k0);
+  FbIn fb;
+  if (FB) fb = fb_load(d, c);
+  float hkm = (k0 == km) ? d.h[c] : 0.f;
+  __syncthreads();
+
+  // the rows of u, v, w in plane kk that this thread's faces read, requested into L1
+  // ahead of time (row 0 also reads the row south of the tile, the top row the row north)
+  auto prefetch_plane = [&](int kk) {
+    const int cp = lix(d, i, j, kk);
+    const float *q[3] = {d.u + cp, d.v + cp, d.w + cp};
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+      asm volatile("prefetch.global.L1 [%0];" ::"l"(q[f]));
+      if (ty == 0 && f == 1) asm volatile("prefetch.global.L1 [%0];" ::"l"(q[f] - d.pi));
+      if (ty == MTY - 1) asm volatile("prefetch.global.L1 [%0];" ::"l"(q[f] + d.pi));
+    }
+  };
+
+  for (int k = k0; k <= k1; ++k) {
+    const bool more = k < k1;
+    if (k + 3 <= km + 1) prefetch_plane(k + 3);
+    // ---- the faces of plane k+1 (j faces into the other half of shared memory) and its
+    // k faces at k+2; the feedbf operands of plane k+1, used after the next combine
+    MFaces Xn = X, Z2 = Z1;
+    unsigned fxyn = 0, fz2 = 0;
+    FbIn fbn;
+    float hkmn = 0.f;
+    if (more) {
+      form(load(k + 1, k + 2), k + 1, k + 2, Xn, Z2, fxyn, fz2);
+      if (FB) fbn = fb_load(d, c + d.np);
+      if (k + 1 == km) hkmn = d.h[c + d.np];
+    }
+    // ---- combine plane k: i faces from the lane to the east, j faces from shared memory
+    unsigned bd = fxy | fz0 | fz1;
+    MFaces B;
+    B.u.nou = __shfl_down_sync(0xffffffffu, X.u.nou, 1);
+    B.u.diu = __shfl_down_sync(0xffffffffu, X.u.diu, 1);
+    B.v.nou = __shfl_down_sync(0xffffffffu, X.v.nou, 1);
+    B.v.diu = __shfl_down_sync(0xffffffffu, X.v.diu, 1);
+    B.w.nou = __shfl_down_sync(0xffffffffu, X.w.nou, 1);
+    B.w.diu = __shfl_down_sync(0xffffffffu, X.w.diu, 1);
+    const MFaces Y0 = ys[k & 1][ty][lane], Y1 = ys[k & 1][ty + 1][lane];
+    VelfgOut o;
+    o.d1 = X.u.diu; o.d2 = Y0.u.diu; o.d3 = Z0.u.diu; o.d3t = Z1.u.diu;
+    o.f = velfg_fu<P2, ZF>(d, i, j, k, X.u, B.u, Y0.u, Y1.u, Z0.u, Z1.u, bd);
+    o.d4 = X.v.diu; o.d5 = Y0.v.diu; o.d6 = Z0.v.diu; o.d6t = Z1.v.diu;
+    o.g = velfg_fv<P2, ZF>(d, i, j, k, X.v, B.v, Y0.v, Y1.v, Z0.v, Z1.v, bd);
+    if (k <= km - 1) {
+      o.d7 = X.w.diu; o.d8 = Y0.w.diu; o.d9 = Z0.w.diu;
+      o.h = velfg_fw<P2, ZF>(d, i, j, k, X.w, B.w, Y0.w, Y1.w, Z0.w, Z1.w, bd);
+    } else {  // k = km: h keeps its value; diu7, diu8 are never written there (zero)
+      o.h = hkm;
+      o.d7 = 0.f;
+      o.d8 = 0.f;
+      o.d9 = Z0.w.diu;
+    }
+    // plane k's j faces are read and plane k+1's written; a plane with a deferred cell is
+    // stored by the fixup kernel (lanes and rows past the domain count: their faces feed
+    // the cells inside)
+    const bool defer = ZF && __syncthreads_or(bd);
+    if (!ZF) __syncthreads();
+    if (defer) {
+      if (lane == 0 && ty == 0) {
+        int *list = d.fix[FIX_VELFG];
+        const int s = atomicAdd(list, 1);
+        list[2 + s] = (int)(((k - 1) * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x);
+      }
+    } else if (in) {
+      velfg_store<FB>(d, c, k, o, fb);
+    }
+    X = Xn;
+    Z0 = Z1;
+    Z1 = Z2;
+    fxy = fxyn;
+    fz0 = fz1;
+    fz1 = fz2;
+    fb = fbn;
+    hkm = hkmn;
+    c += d.np;
+  }
 }
-// the deferred blocks of k_velfg2<P2, true, FB>, with IEEE divisions
+
+// deferred planes of k_velfg_march: entry ((k-1)*gy + by)*gx + bx, recomputed cell by
+// cell with IEEE divisions
 template <bool P2, bool FB>
-__global__ void __launch_bounds__(FX *FY *FZ) k_velfg2_fix(LesDom d, uint3 g) {
-  for_deferred(d.fix[FIX_VELFG], g, [&](int bx, int by, int bz) { velfg_block<P2, false, FB>(d, bx, by, bz); });
+__global__ void __launch_bounds__(MTX *MTY) k_velfg_march_fix(LesDom d, uint3 g) {
+  for_deferred(d.fix[FIX_VELFG], g, [&](int bx, int by, int bz) {
+    const int i = bx * MTI + (int)threadIdx.x + 1, j = by * MTY + (int)threadIdx.y + 1, k = bz + 1;
+    if ((int)threadIdx.x >= MTI || i > d.im || j > d.jm) return;
+    const int c = lix(d, i, j, k);
+    FbIn fb;
+    if (FB) fb = fb_load(d, c);
+    VelfgOut o;
+    unsigned bd = 0;
+    velfg_cell<P2, false>(d, i, j, k, c, o, bd);
+    velfg_store<FB>(d, c, k, o, fb);
+  });
 }
 
 #define SM_(i, j, k) __ldg(&d.sm[lix(d, (i), (j), (k))])
@@ -696,33 +919,33 @@ inline dim3 fgrid(const LesDom &d) { return dim3((d.im + FX - 1) / FX, (d.jm + F
 namespace {
 // Launch a fused kernel K<P2, ZF, X> for the domain's spacing modes; with ZF its fixup
 // kernel F<P2, X> follows (it does nothing when no block was deferred).
-template <template <bool, bool, bool> class K, template <bool, bool> class F>
-void launch_variant(const LesDom &d, bool x, LesCtx ctx, dim3 g, dim3 b) {
+template <template <bool, bool, bool> class K, template <bool, bool> class F, typename... Args>
+void launch_variant(const LesDom &d, bool x, LesCtx ctx, dim3 g, dim3 b, Args... args) {
   const uint3 gu = make_uint3(g.x, g.y, g.z);
   const unsigned nfix = std::min<unsigned>(g.x * g.y * g.z, (unsigned)std::max(1, 2 * d.sms));
   const int v = (d.xy_pow2 ? 4 : 0) | (d.zfast ? 2 : 0) | (x ? 1 : 0);
   switch (v) {
-    case 0: LAUNCH(ctx, (K<false, false, false>::fn<<<g, b, 0, ctx.s>>>(d))); break;
-    case 1: LAUNCH(ctx, (K<false, false, true>::fn<<<g, b, 0, ctx.s>>>(d))); break;
-    case 2: LAUNCH(ctx, (K<false, true, false>::fn<<<g, b, 0, ctx.s>>>(d)));
+    case 0: LAUNCH(ctx, (K<false, false, false>::fn<<<g, b, 0, ctx.s>>>(d, args...))); break;
+    case 1: LAUNCH(ctx, (K<false, false, true>::fn<<<g, b, 0, ctx.s>>>(d, args...))); break;
+    case 2: LAUNCH(ctx, (K<false, true, false>::fn<<<g, b, 0, ctx.s>>>(d, args...)));
             LAUNCH(ctx, (F<false, false>::fn<<<nfix, b, 0, ctx.s>>>(d, gu))); break;
-    case 3: LAUNCH(ctx, (K<false, true, true>::fn<<<g, b, 0, ctx.s>>>(d)));
+    case 3: LAUNCH(ctx, (K<false, true, true>::fn<<<g, b, 0, ctx.s>>>(d, args...)));
             LAUNCH(ctx, (F<false, true>::fn<<<nfix, b, 0, ctx.s>>>(d, gu))); break;
-    case 4: LAUNCH(ctx, (K<true, false, false>::fn<<<g, b, 0, ctx.s>>>(d))); break;
-    case 5: LAUNCH(ctx, (K<true, false, true>::fn<<<g, b, 0, ctx.s>>>(d))); break;
-    case 6: LAUNCH(ctx, (K<true, true, false>::fn<<<g, b, 0, ctx.s>>>(d)));
+    case 4: LAUNCH(ctx, (K<true, false, false>::fn<<<g, b, 0, ctx.s>>>(d, args...))); break;
+    case 5: LAUNCH(ctx, (K<true, false, true>::fn<<<g, b, 0, ctx.s>>>(d, args...))); break;
+    case 6: LAUNCH(ctx, (K<true, true, false>::fn<<<g, b, 0, ctx.s>>>(d, args...)));
             LAUNCH(ctx, (F<true, false>::fn<<<nfix, b, 0, ctx.s>>>(d, gu))); break;
-    default: LAUNCH(ctx, (K<true, true, true>::fn<<<g, b, 0, ctx.s>>>(d)));
+    default: LAUNCH(ctx, (K<true, true, true>::fn<<<g, b, 0, ctx.s>>>(d, args...)));
              LAUNCH(ctx, (F<true, true>::fn<<<nfix, b, 0, ctx.s>>>(d, gu))); break;
   }
 }
 template <bool A, bool B, bool C>
 struct VelfgK {
-  static constexpr auto fn = k_velfg2<A, B, C>;
+  static constexpr auto fn = k_velfg_march<A, B, C>;
 };
 template <bool A, bool C>
 struct VelfgF {
-  static constexpr auto fn = k_velfg2_fix<A, C>;
+  static constexpr auto fn = k_velfg_march_fix<A, C>;
 };
 template <bool A, bool B, bool C>
 struct ViscK {
@@ -734,9 +957,25 @@ struct ViscF {
 };
 }  // namespace
 
+// Planes per block of the velfg march: chunks enough for about twelve blocks per SM,
+// of 6 to 20 planes (a chunk re-forms the faces of its first plane).
+static int velfg_kchunk(const LesDom &d) {
+  if (const char *e = getenv("LES_VELFG_KCHUNK")) {  // A/B measurements
+    const int v = atoi(e);
+    if (v > 0) return std::min(v, d.km);
+  }
+  const long long tiles = (long long)((d.im + MTI - 1) / MTI) * ((d.jm + MTY - 1) / MTY);
+  const int sms = d.sms > 0 ? d.sms : 152;
+  const int nch = (int)std::max<long long>(1, (12LL * sms + tiles - 1) / tiles);
+  const int kc = (d.km + nch - 1) / nch;
+  return std::min(d.km, std::max(6, std::min(20, kc)));
+}
+
 void les_launch_velfg_fused(const LesDom &d, bool with_feedbf, LesCtx ctx) {
   LAUNCH(ctx, (k_wall<<<dim3((d.im + 127) / 128, d.jm), 128, 0, ctx.s>>>(d)));
-  launch_variant<VelfgK, VelfgF>(d, with_feedbf, ctx, fgrid(d), dim3(FX, FY, FZ));
+  const int kc = velfg_kchunk(d);
+  const dim3 g((d.im + MTI - 1) / MTI, (d.jm + MTY - 1) / MTY, (d.km + kc - 1) / kc);
+  launch_variant<VelfgK, VelfgF>(d, with_feedbf, ctx, g, dim3(MTX, MTY), kc);
 }
 
 void les_launch_les_fused(const LesDom &d, bool with_adam, LesCtx ctx) {

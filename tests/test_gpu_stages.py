@@ -66,6 +66,17 @@ def test_velfg(built_lib, shape, spacing):
     _assert_same(gpu, orc, STATE, "velfg")
 
 
+@pytest.mark.parametrize("kchunk", [1, 3, 7])
+def test_velfg_march_chunks(built_lib, monkeypatch, kchunk):
+    """The velfg k-march split into chunks of planes (each re-forming the faces of its
+    first plane): bit for bit the oracle's, with tiles partial in i (70 = 2 x 31 + 8)
+    and in j (20 = 2 x 8 + 4)."""
+    monkeypatch.setenv("LES_VELFG_KCHUNK", str(kchunk))
+    sc, gpu, orc = _pair((70, 20, 10), spacing=(3.0, 5.0))
+    gpu.velfg(); orc.stage(ref.VELFG)
+    _assert_same(gpu, orc, STATE, f"velfg kchunk={kchunk}")
+
+
 @pytest.mark.parametrize("shape", SHAPES)
 def test_feedbf(built_lib, shape):
     sc, gpu, orc = _pair(shape)
