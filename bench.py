@@ -320,7 +320,11 @@ def run_ours(args):
     cells = IM * JM * KM
     dom = lesgpu.Domain(IM, JM, KM, lesgpu.Params())
     dom.setup_scenario(scenario(seed=1 + rank, im=IM, jm=JM, km=KM))
-    sor_shape, sor_tuned_us, _ = dom.tune_sor(False)  # measured SOR tile shape (untimed set-up)
+    if args.sor_shape:
+        dom.set_sor_shape(*(int(x) for x in args.sor_shape.lower().split("x")))
+        sor_shape, sor_tuned_us = dom.sor_shape(), None
+    else:
+        sor_shape, sor_tuned_us, _ = dom.tune_sor(False)  # measured SOR tile shape (untimed set-up)
     stream = torch.cuda.ExternalStream(dom.stream())
     nmax = args.warmup + args.steps + 10**6
     n = 1
@@ -506,6 +510,9 @@ def main():
     ap.add_argument("--dims", default=f"{IM}x{JM}x{KM}", help="domain IMxJMxKM (default: the workload's)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-ensemble measurements")
+    ap.add_argument("--sor-shape", default=None,
+                    help="NXxNYxKCHUNK: fix the SOR tile shape instead of tuning it (for runs under a profiler, "
+                         "whose timings would mislead the tuner)")
     ap.add_argument("--mode", default="plain", choices=["plain", "serve"])
     ap.add_argument("--serve-seconds", type=float, default=120.0, help="serve mode: arrival window")
     ap.add_argument("--rate", type=float, default=20.0, help="serve mode: requests per second")
