@@ -476,6 +476,9 @@ def run_serve(args):
                     probes[r.rid] = {fid: dom.download(fid, (1, 1, 1), (r.im, r.jm, r.km))
                                      for fid in (lesgpu.U, lesgpu.V, lesgpu.W, lesgpu.P)}
 
+    t_tune = time.perf_counter()
+    tuned = be.pretune(reqs)  # the SOR shape of each size class, with the GPU idle
+    t_tune = time.perf_counter() - t_tune
     srv = serve.Server(be, max_live=256, setup_workers=4, on_step=on_step)
     with ClockSampler(0) as clk:
         st = srv.run(reqs)
@@ -492,6 +495,7 @@ def run_serve(args):
             "completed": st["completed"], "rejected": st["rejected"], "wall_s": st["wall_s"],
             "max_backlog": st["max_backlog"], "batch_iterations": st["batch_iterations"],
             "mean_live_cells": st["mean_live_cells"], "clocks": clk.summary(),
+            "sor_tuning": {"classes": len(tuned), "seconds": t_tune, "before": "the arrival window"},
             "oracle_check": {"requests": len(errs), "steps": check_steps, "max_rel_err": max(errs) if errs else None,
                              "sample": f"every 20th request (5 percent), the first {args.check} of them; u, v, w, "
                                        f"p after {check_steps} steps vs the FP64 oracle"}}

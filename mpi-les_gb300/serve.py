@@ -80,6 +80,24 @@ class GpuBackend:
         self.inflight = 0  # bytes of admitted domains whose set-up has not allocated yet
         self.lock = threading.Lock()
 
+    def pretune(self, requests: list[Request]) -> dict:
+        """Tune the SOR tile shape of every size class among `requests` for a shared GPU
+        (les_gpu_tune_sor), before serving starts: tuning needs an otherwise idle GPU.
+        One scratch domain per class; returns {(im, jm, km): (shape, us)}."""
+        done = {}
+        for r in requests:
+            key = (r.im, r.jm, r.km)
+            if key in done or self.lesgpu.sor_tuned(*key, True) is not None:
+                continue
+            d = self.lesgpu.Domain(r.im, r.jm, r.km, self.params)
+            try:
+                d.setup_scenario(self.scenario(r))
+                shape, us, _ = d.tune_sor(True)
+                done[key] = (shape, us)
+            finally:
+                d.close()
+        return done
+
     def footprint(self, r: Request) -> int:
         return int(self.lesgpu.load_library().les_domain_bytes(r.im, r.jm, r.km))
 
