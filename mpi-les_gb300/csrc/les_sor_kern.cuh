@@ -75,11 +75,13 @@ __device__ __forceinline__ float relax_pair(int q, float4 &cur, float pl, float 
 }
 
 // Per-thread geometry shared by both kernels.
+constexpr int NO_GHOST = -1000;
 struct Lane {
   int c4, r, ib, jr, jw;
   bool row_owned, row_red, col_owned, owned, west0;
   int east_e;
   bool ival[4];
+  int ghost1, ghost2;  // periodic ghost rows that copy row jr (NO_GHOST: none)
 };
 
 template <int NX>
@@ -105,6 +107,10 @@ __device__ __forceinline__ Lane make_lane(const LesDom &d, int tj, int ny) {
   L.east_e = d.im - L.ib;
 #pragma unroll
   for (int e = 0; e < 4; ++e) L.ival[e] = (L.ib + e >= 1) && (L.ib + e <= d.im);
+  // row 1 -> jm+1, row 2 -> jm+2, row jm-1 -> -1, row jm -> 0 (jm = 2: two ghosts per row)
+  const int jm = d.jm;
+  L.ghost1 = (L.jr == 1) ? jm + 1 : (L.jr == 2) ? jm + 2 : NO_GHOST;
+  L.ghost2 = (L.jr == jm - 1) ? -1 : (L.jr == jm) ? 0 : NO_GHOST;
   return L;
 }
 
@@ -124,11 +130,8 @@ __device__ __forceinline__ void store_final(const LesDom &d, const SorArgs &a, c
   };
   put(L.jr);
   if (a.ghost) {
-    const int jm = d.jm;
-    if (L.jr == 1) put(jm + 1);
-    if (L.jr == 2) put(jm + 2);
-    if (L.jr == jm - 1) put(-1);
-    if (L.jr == jm) put(0);
+    if (L.ghost1 != NO_GHOST) put(L.ghost1);
+    if (L.ghost2 != NO_GHOST) put(L.ghost2);
   }
 }
 
@@ -469,33 +472,45 @@ __global__ void __launch_bounds__(NX *NY, min_ctas(NX))
     for (int m = mfirst; m < mfirst + D && m <= mlast; ++m) issue(m);
 
   int failed_at = 0;
-  auto wait_plane = [&](int m) {
-    if (!mbar_wait(&S.bar[(m - mfirst) % D], (uint32_t)(((m - mfirst) / D) & 1))) {
+  // plane m sits in stage (m - mfirst) % D with mbarrier phase parity ((m - mfirst) / D) & 1
+  auto wait_stage = [&](int m, int st, uint32_t ph) {
+    if (!mbar_wait(&S.bar[st], ph)) {
       S.abort_ = 1;
       d.ctl[CT_ERROR] = 1;
       if (!failed_at) failed_at = m;
     }
   };
+  auto wait_plane = [&](int m) { wait_stage(m, (m - mfirst) % D, (uint32_t)(((m - mfirst) / D) & 1)); };
 
   const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
   float4 Pm2 = zero4, Pm1 = zero4, P0 = zero4, Rm1 = zero4;
+  wait_plane(s_begin);
+  P0 = S.p[(s_begin - mfirst) % D][r][c4];
+  // plane 0 reads as plane 1 (boundp2's Neumann copy): with Pm1 a copy of plane 1 taken
+  // before its red update, every k-halo read below finds the cell's own current value
+  // (red at s = 1 reads Pm1, black at k = 1 reads the same copy two steps later, and at
+  // the top P1 = P0 when plane km+1 would be next), so the march needs no halo selects
+  Pm1 = P0;
   if (KC && s_begin > 1) {
     wait_plane(s_begin - 1);
     Pm1 = S.p[(s_begin - 1 - mfirst) % D][r][c4];
   }
-  wait_plane(s_begin);
-  P0 = S.p[(s_begin - mfirst) % D][r][c4];
   float acc = 0.f, comp = 0.f;
+  // stage and phase of plane s (st0) and of plane s+1 (st1, ph1), advanced per step
+  int st0 = (s_begin - mfirst) % D, st1 = (s_begin + 1 - mfirst) % D;
+  uint32_t ph1 = (uint32_t)(((s_begin + 1 - mfirst) / D) & 1);
+  // this plane's coefficients (plane s) and the previous plane's (black of s-1)
+  float ck0 = 0.f, c4l0 = 0.f, c4s0 = 0.f, ckm = 0.f, c4lm = 0.f, c4sm = 0.f;
 
   for (int s = s_begin; s <= s_end; ++s) {
     __syncthreads();
     if (S.abort_) continue;
     // the stage of plane s-1 is free: every thread has left step s-1 (or the prologue)
     if (producer && s - 1 >= mfirst && s - 1 + D <= mlast) issue(s - 1 + D);
-    float4 P1 = P0, R0 = zero4;
+    float4 P1 = P0, R0 = zero4;  // plane km+1 reads as plane km, before its red update
     if (s + 1 <= mlast) {
-      wait_plane(s + 1);
-      P1 = S.p[(s + 1 - mfirst) % D][r][c4];
+      wait_stage(s + 1, st1, ph1);
+      P1 = S.p[st1][r][c4];
     }
     float part = 0.f;
     const int B = s & 1, BB = (s - 1) & 1;
@@ -505,26 +520,23 @@ __global__ void __launch_bounds__(NX *NY, min_ctas(NX))
     const float rpr = __shfl_down_sync(0xffffffffu, P0.x, 1, NX);
     const float bpl = __shfl_up_sync(0xffffffffu, Pm1.w, 1, NX);
     const float bpr = __shfl_down_sync(0xffffffffu, Pm1.x, 1, NX);
-    if (s <= km && L.row_red) {
-      const int st = (s - mfirst) % D;
-      R0 = S.rhs[st][r][c4];
-      const float4 pn = S.p[st][r + 1][c4], pso = S.p[st][r - 1][c4];
-      const float pl = rpl, pr = rpr;
-      // virtual k halos: p(0) = p(1), p(km+1) = p(km) (the cell's own value)
-      const float4 up = (s == km) ? P0 : P1;
-      const float4 dn = (s == 1) ? P0 : Pm1;
-      part += relax_pair(q, P0, pl, pr, pn, pso, up, dn, R0, rhsav, omega, S.ck[s], c2l, c2s, c3l, c3s,
-                         S.c4l[s], S.c4s[s], L.west0, L.east_e, L.owned && (!KC || (s >= ka && s <= kb)), L.ival);
+    if (s <= km) {
+      ck0 = S.ck[s];
+      c4l0 = S.c4l[s];
+      c4s0 = S.c4s[s];
+      if (L.row_red) {
+        R0 = S.rhs[st0][r][c4];
+        const float4 pn = S.p[st0][r + 1][c4], pso = S.p[st0][r - 1][c4];
+        part += relax_pair(q, P0, rpl, rpr, pn, pso, P1, Pm1, R0, rhsav, omega, ck0, c2l, c2s, c3l, c3s, c4l0, c4s0,
+                           L.west0, L.east_e, L.owned && (!KC || (s >= ka && s <= kb)), L.ival);
+      }
     }
     S.red[B][r][c4] = P0;
     if ((KC ? (s - 1 >= ka && s - 1 <= kb) : (s >= 2)) && L.owned) {
       const int k = s - 1;
       const float4 pn = S.red[BB][r + 1][c4], pso = S.red[BB][r - 1][c4];
-      const float pl = bpl, pr = bpr;
-      const float4 up = (k == km) ? Pm1 : P0;
-      const float4 dn = (k == 1) ? Pm1 : Pm2;
-      part += relax_pair(q, Pm1, pl, pr, pn, pso, up, dn, Rm1, rhsav, omega, S.ck[k], c2l, c2s, c3l, c3s,
-                         S.c4l[k], S.c4s[k], L.west0, L.east_e, true, L.ival);
+      part += relax_pair(q, Pm1, bpl, bpr, pn, pso, P0, Pm2, Rm1, rhsav, omega, ckm, c2l, c2s, c3l, c3s, c4lm, c4sm,
+                         L.west0, L.east_e, true, L.ival);
       store_final(d, a, L, k, Pm1);
     }
     {
@@ -537,6 +549,14 @@ __global__ void __launch_bounds__(NX *NY, min_ctas(NX))
     Pm1 = P0;
     P0 = P1;
     Rm1 = R0;
+    ckm = ck0;
+    c4lm = c4l0;
+    c4sm = c4s0;
+    st0 = st1;
+    if (++st1 == D) {
+      st1 = 0;
+      ph1 ^= 1u;
+    }
   }
   // after a failed wait, wait (bounded) for the copies already issued before leaving
   if (failed_at) {
