@@ -283,6 +283,7 @@ __global__ void __launch_bounds__(NX *NY, min_ctas(NX)) k_sor_reg(LesDom d, SorA
     const int q = (jw + s) & 1;
     // ---- red cells of plane s on tile + 1-cell ring
     // i-neighbours of the float4 edges from the adjacent lanes (NX lanes are a tile row)
+    // i-neighbours of the float4 edges from the adjacent lanes (NX lanes are a tile row)
     const float rpl = __shfl_up_sync(0xffffffffu, P[S0].w, 1, NX);
     const float rpr = __shfl_down_sync(0xffffffffu, P[S0].x, 1, NX);
     const float bpl = __shfl_up_sync(0xffffffffu, P[SM1].w, 1, NX);
@@ -482,81 +483,102 @@ __global__ void __launch_bounds__(NX *NY, min_ctas(NX))
   };
   auto wait_plane = [&](int m) { wait_stage(m, (m - mfirst) % D, (uint32_t)(((m - mfirst) / D) & 1)); };
 
+  // Plane m of p lives in register slot P[m % 4] and its rhs and coefficients in slot
+  // m % 2; the march is unrolled 4 times so every slot is a compile-time register and
+  // the planes never move between registers.  Plane 0 reads as plane 1 (boundp2's
+  // Neumann copy): with slot s_begin-1 a copy of plane 1 taken before its red update,
+  // every k-halo read below finds the cell's own current value (red at s = 1 reads that
+  // copy, black at k = 1 reads it one step later, and at the top the slot of plane
+  // km+1 is a copy of plane km), so the march needs no halo selects.
   const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
-  float4 Pm2 = zero4, Pm1 = zero4, P0 = zero4, Rm1 = zero4;
-  wait_plane(s_begin);
-  P0 = S.p[(s_begin - mfirst) % D][r][c4];
-  // plane 0 reads as plane 1 (boundp2's Neumann copy): with Pm1 a copy of plane 1 taken
-  // before its red update, every k-halo read below finds the cell's own current value
-  // (red at s = 1 reads Pm1, black at k = 1 reads the same copy two steps later, and at
-  // the top P1 = P0 when plane km+1 would be next), so the march needs no halo selects
-  Pm1 = P0;
-  if (KC && s_begin > 1) {
-    wait_plane(s_begin - 1);
-    Pm1 = S.p[(s_begin - 1 - mfirst) % D][r][c4];
+  float4 P[4], R[2];
+  float CK[2] = {0.f, 0.f}, C4L[2] = {0.f, 0.f}, C4S[2] = {0.f, 0.f};
+#pragma unroll
+  for (int t = 0; t < 4; ++t) P[t] = zero4;
+  R[0] = R[1] = zero4;
+  {
+    wait_plane(s_begin);
+    const float4 p0 = S.p[(s_begin - mfirst) % D][r][c4];
+    float4 pm1 = p0;
+    if (KC && s_begin > 1) {
+      wait_plane(s_begin - 1);
+      pm1 = S.p[(s_begin - 1 - mfirst) % D][r][c4];
+    }
+    const int t0 = s_begin % 4, t1 = (s_begin + 3) % 4;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      if (t == t0) P[t] = p0;
+      if (t == t1) P[t] = pm1;
+    }
   }
   float acc = 0.f, comp = 0.f;
   // stage and phase of plane s (st0) and of plane s+1 (st1, ph1), advanced per step
   int st0 = (s_begin - mfirst) % D, st1 = (s_begin + 1 - mfirst) % D;
   uint32_t ph1 = (uint32_t)(((s_begin + 1 - mfirst) / D) & 1);
-  // this plane's coefficients (plane s) and the previous plane's (black of s-1)
-  float ck0 = 0.f, c4l0 = 0.f, c4s0 = 0.f, ckm = 0.f, c4lm = 0.f, c4sm = 0.f;
 
-  for (int s = s_begin; s <= s_end; ++s) {
+  auto step = [&](auto UC, int s) {
+    constexpr int U = decltype(UC)::value;  // s = U modulo 4
+    constexpr int S0 = U, SP1 = (U + 1) % 4, SM1 = (U + 3) % 4, SM2 = (U + 2) % 4;
+    constexpr int C0 = U % 2, CM = (U + 1) % 2;
+    if (s < s_begin) return;  // before this chunk's start (the unrolled march is aligned to 4)
     __syncthreads();
-    if (S.abort_) continue;
+    if (S.abort_) return;
     // the stage of plane s-1 is free: every thread has left step s-1 (or the prologue)
     if (producer && s - 1 >= mfirst && s - 1 + D <= mlast) issue(s - 1 + D);
-    float4 P1 = P0, R0 = zero4;  // plane km+1 reads as plane km, before its red update
+    P[SP1] = P[S0];  // plane km+1 reads as plane km, before its red update
+    R[C0] = zero4;
     if (s + 1 <= mlast) {
       wait_stage(s + 1, st1, ph1);
-      P1 = S.p[st1][r][c4];
+      P[SP1] = S.p[st1][r][c4];
     }
     float part = 0.f;
-    const int B = s & 1, BB = (s - 1) & 1;
     const int q = (jw + s) & 1;
-    // i-neighbours of the float4 edges from the adjacent lanes (NX lanes are a tile row)
-    const float rpl = __shfl_up_sync(0xffffffffu, P0.w, 1, NX);
-    const float rpr = __shfl_down_sync(0xffffffffu, P0.x, 1, NX);
-    const float bpl = __shfl_up_sync(0xffffffffu, Pm1.w, 1, NX);
-    const float bpr = __shfl_down_sync(0xffffffffu, Pm1.x, 1, NX);
+    const float rpl = __shfl_up_sync(0xffffffffu, P[S0].w, 1, NX);
+    const float rpr = __shfl_down_sync(0xffffffffu, P[S0].x, 1, NX);
+    const float bpl = __shfl_up_sync(0xffffffffu, P[SM1].w, 1, NX);
+    const float bpr = __shfl_down_sync(0xffffffffu, P[SM1].x, 1, NX);
+    // ---- red cells of plane s on the tile + 1-cell ring
     if (s <= km) {
-      ck0 = S.ck[s];
-      c4l0 = S.c4l[s];
-      c4s0 = S.c4s[s];
+      CK[C0] = S.ck[s];
+      C4L[C0] = S.c4l[s];
+      C4S[C0] = S.c4s[s];
       if (L.row_red) {
-        R0 = S.rhs[st0][r][c4];
+        R[C0] = S.rhs[st0][r][c4];
         const float4 pn = S.p[st0][r + 1][c4], pso = S.p[st0][r - 1][c4];
-        part += relax_pair(q, P0, rpl, rpr, pn, pso, P1, Pm1, R0, rhsav, omega, ck0, c2l, c2s, c3l, c3s, c4l0, c4s0,
-                           L.west0, L.east_e, L.owned && (!KC || (s >= ka && s <= kb)), L.ival);
+        part += relax_pair(q, P[S0], rpl, rpr, pn, pso, P[SP1], P[SM1], R[C0], rhsav, omega, CK[C0], c2l, c2s, c3l,
+                           c3s, C4L[C0], C4S[C0], L.west0, L.east_e, L.owned && (!KC || (s >= ka && s <= kb)),
+                           L.ival);
       }
     }
-    S.red[B][r][c4] = P0;
+    S.red[U & 1][r][c4] = P[S0];
+    // ---- black cells of plane s-1 on the tile
     if ((KC ? (s - 1 >= ka && s - 1 <= kb) : (s >= 2)) && L.owned) {
       const int k = s - 1;
-      const float4 pn = S.red[BB][r + 1][c4], pso = S.red[BB][r - 1][c4];
-      part += relax_pair(q, Pm1, bpl, bpr, pn, pso, P0, Pm2, Rm1, rhsav, omega, ckm, c2l, c2s, c3l, c3s, c4lm, c4sm,
-                         L.west0, L.east_e, true, L.ival);
-      store_final(d, a, L, k, Pm1);
+      const float4 pn = S.red[(U + 1) & 1][r + 1][c4], pso = S.red[(U + 1) & 1][r - 1][c4];
+      part += relax_pair(q, P[SM1], bpl, bpr, pn, pso, P[S0], P[SM2], R[CM], rhsav, omega, CK[CM], c2l, c2s, c3l,
+                         c3s, C4L[CM], C4S[CM], L.west0, L.east_e, true, L.ival);
+      store_final(d, a, L, k, P[SM1]);
     }
-    {
+    {  // Kahan accumulation of this step's squared corrections
       const float y = part - comp;
       const float t = acc + y;
       comp = (t - acc) - y;
       acc = t;
     }
-    Pm2 = Pm1;
-    Pm1 = P0;
-    P0 = P1;
-    Rm1 = R0;
-    ckm = ck0;
-    c4lm = c4l0;
-    c4sm = c4s0;
     st0 = st1;
     if (++st1 == D) {
       st1 = 0;
       ph1 ^= 1u;
     }
+  };
+  for (int s0 = s_begin - s_begin % 4; s0 <= s_end; s0 += 4) {
+    step(IC<0>{}, s0);
+    if (s0 + 1 > s_end) break;
+    step(IC<1>{}, s0 + 1);
+    if (s0 + 2 > s_end) break;
+    step(IC<2>{}, s0 + 2);
+    if (s0 + 3 > s_end) break;
+    step(IC<3>{}, s0 + 3);
   }
   // after a failed wait, wait (bounded) for the copies already issued before leaving
   if (failed_at) {
