@@ -152,6 +152,16 @@ int les_gpu_upload(les_handle *h, int field, const float *host, const int lb[3],
                    const int ub[3]);
 int les_gpu_download(les_handle *h, int field, float *host, const int lb[3],
                      const int ub[3]);
+/* Asynchronous download of a 3-D field's box (no reference counterpart: it lets the
+ * per-step output of main.f95:311-327 overlap the next step).  The box is snapshotted on
+ * the device in stream order -- later steps may be queued at once and do not change
+ * what is copied -- and copied to `host` on a copy stream of the handle.  *ticket
+ * identifies the copy; les_gpu_download_wait(h, ticket) returns once it is in host
+ * memory.  `host` must stay valid until then (pinned memory lets the copy overlap).
+ * At most 8 copies are in flight per handle: a ninth call first waits for the oldest. */
+int les_gpu_download_async(les_handle *h, int field, float *host, const int lb[3], const int ub[3],
+                           long long *ticket);
+int les_gpu_download_wait(les_handle *h, long long ticket);
 /* Validate the uploaded grid/coefficients/masks/inflow and derive the per-domain
  * constants (les.f95:38-42 delx1, the log-law factor of vel2.f95:138).  Required
  * once before the first solver call and after any later grid upload. */

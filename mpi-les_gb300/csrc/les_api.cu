@@ -103,6 +103,18 @@ struct les_handle {
   long long nlaunch = 0;
   std::string err;
   LesStepPlan plan{};
+  // downloads: a box is packed on h->s into a staging slot, then copied to the host on
+  // the copy stream cs (les_gpu_download_async); slots are reused in ticket order
+  struct DlSlot {
+    float *buf = nullptr;
+    size_t cap = 0;  // floats
+    cudaEvent_t packed = nullptr, done = nullptr;
+    long long ticket = -1;
+  };
+  static constexpr int kDlSlots = 8;
+  DlSlot dl[kDlSlots];
+  cudaStream_t cs = nullptr;
+  long long next_ticket = 0;
 };
 
 namespace {
@@ -246,6 +258,13 @@ extern "C" int les_gpu_create(const les_dims *dims, const les_params *params, le
 extern "C" int les_gpu_destroy(les_handle *h) {
   if (!h) return LES_OK;
   if (h->s) cudaStreamSynchronize(h->s);
+  if (h->cs) cudaStreamSynchronize(h->cs);
+  for (auto &sl : h->dl) {
+    cudaFree(sl.buf);
+    if (sl.packed) cudaEventDestroy(sl.packed);
+    if (sl.done) cudaEventDestroy(sl.done);
+  }
+  if (h->cs) cudaStreamDestroy(h->cs);
   les_step_plan_free(&h->plan);
   for (int f = 0; f < kNumFields; ++f) cudaFree(h->fields[f]);
   cudaFree(h->mask_d);
@@ -355,16 +374,88 @@ extern "C" int les_gpu_upload(les_handle *h, int field, const float *host, const
   return LES_OK;
 }
 
+namespace {
+
+// Box (i0.., j0.., k0.., nx x ny) x nz of a padded field into a contiguous array in
+// Fortran order: one row of the box (fixed j, k) per block.
+__global__ void k_pack_box(const float *__restrict__ src, float *__restrict__ dst, int pi, int nj, int i0, int j0,
+                           int k0, int nx, int ny) {
+  const int row = blockIdx.x;  // (j - j0) + ny * (k - k0)
+  const int jj = row % ny, kk = row / ny;
+  const float *s = src + ((size_t)(k0 + kk + LES_KOFF) * nj + (j0 + jj + LES_JOFF)) * pi + (i0 + LES_IOFF);
+  float *o = dst + (size_t)row * nx;
+  for (int i = threadIdx.x; i < nx; i += blockDim.x) o[i] = s[i];
+}
+
+// Snapshot the box on h->s and queue its copy to `host` on the copy stream.
+int download_async(les_handle *h, int field, float *host, const int lb[3], const int ub[3], long long *ticket) {
+  const int nx = ub[0] - lb[0] + 1, ny = ub[1] - lb[1] + 1, nz = ub[2] - lb[2] + 1;
+  const size_t n = (size_t)nx * ny * nz;
+  if (!h->cs) CK(h, cudaStreamCreateWithFlags(&h->cs, cudaStreamNonBlocking));
+  const long long t = h->next_ticket++;
+  les_handle::DlSlot &sl = h->dl[t % les_handle::kDlSlots];
+  if (!sl.done) {
+    CK(h, cudaEventCreateWithFlags(&sl.packed, cudaEventDisableTiming));
+    CK(h, cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming));
+  }
+  // the slot's previous copy must be in host memory before its staging is rewritten
+  if (sl.ticket >= 0) CK(h, cudaEventSynchronize(sl.done));
+  if (sl.cap < n) {
+    cudaFree(sl.buf);
+    sl.buf = nullptr;
+    sl.cap = 0;
+    CK(h, cudaMalloc(&sl.buf, n * sizeof(float)));
+    sl.cap = n;
+  }
+  const unsigned rows = (unsigned)ny * (unsigned)nz;
+  if (rows > 0) {
+    k_pack_box<<<rows, 128, 0, h->s>>>(h->fields[field - 1], sl.buf, h->pi, h->nj, lb[0], lb[1], lb[2], nx, ny);
+    CK(h, cudaGetLastError());
+  }
+  CK(h, cudaEventRecord(sl.packed, h->s));
+  CK(h, cudaStreamWaitEvent(h->cs, sl.packed, 0));
+  CK(h, cudaMemcpyAsync(host, sl.buf, n * sizeof(float), cudaMemcpyDeviceToHost, h->cs));
+  CK(h, cudaEventRecord(sl.done, h->cs));
+  sl.ticket = t;
+  *ticket = t;
+  return LES_OK;
+}
+
+int download_wait(les_handle *h, long long ticket) {
+  if (ticket < 0 || ticket >= h->next_ticket) return fail(h, LES_ERR_ARG, "unknown download ticket");
+  const les_handle::DlSlot &sl = h->dl[ticket % les_handle::kDlSlots];
+  // a slot reused since then waited for this ticket's copy before it was reused
+  if (sl.ticket == ticket) CK(h, cudaEventSynchronize(sl.done));
+  return LES_OK;
+}
+
+}  // namespace
+
+extern "C" int les_gpu_download_async(les_handle *h, int field, float *host, const int lb[3], const int ub[3],
+                                      long long *ticket) {
+  if (!h || !host || !lb || !ub || !ticket) return LES_ERR_ARG;
+  Ext decl;
+  int rc = check_ext(h, field, lb, ub, &decl);
+  if (rc) return rc;
+  if (field < LES_FIELD_U || field > LES_FIELD_SM) return fail(h, LES_ERR_ARG, "download_async: 3-D fields only");
+  return download_async(h, field, host, lb, ub, ticket);
+}
+
+extern "C" int les_gpu_download_wait(les_handle *h, long long ticket) {
+  if (!h) return LES_ERR_ARG;
+  return download_wait(h, ticket);
+}
+
 extern "C" int les_gpu_download(les_handle *h, int field, float *host, const int lb[3], const int ub[3]) {
   if (!h || !host || !lb || !ub) return LES_ERR_ARG;
   Ext decl;
   int rc = check_ext(h, field, lb, ub, &decl);
   if (rc) return rc;
   if (field >= LES_FIELD_U && field <= LES_FIELD_SM) {
-    cudaMemcpy3DParms p = copy_parms(h, h->fields[field - 1], host, lb, ub, false);
-    CK(h, cudaMemcpy3DAsync(&p, h->s));
-    CK(h, cudaStreamSynchronize(h->s));
-    return LES_OK;
+    long long t = -1;
+    rc = download_async(h, field, host, lb, ub, &t);
+    if (rc) return rc;
+    return download_wait(h, t);
   }
   if (field == LES_FIELD_DELX1) {
     if (!h->committed) return fail(h, LES_ERR_STATE, "delx1 is derived at commit");

@@ -159,6 +159,8 @@ def load_library(path: str | None = None) -> C.CDLL:
         "les_gpu_destroy": (C.c_int, [vp]),
         "les_gpu_upload": (C.c_int, [vp, C.c_int, fp_, ip_, ip_]),
         "les_gpu_download": (C.c_int, [vp, C.c_int, fp_, ip_, ip_]),
+        "les_gpu_download_async": (C.c_int, [vp, C.c_int, fp_, ip_, ip_, C.POINTER(C.c_longlong)]),
+        "les_gpu_download_wait": (C.c_int, [vp, C.c_longlong]),
         "les_gpu_commit_setup": (C.c_int, [vp]),
         "les_gpu_setup_scenario": (C.c_int, [vp, C.POINTER(LesScenario)]),
         "les_gpu_velnw": (C.c_int, [vp]),
@@ -328,6 +330,25 @@ class Domain:
         out = np.zeros(shape, np.float32, order="F")
         self._check(self.lib.les_gpu_download(self._h, fid, _fptr(out), _iarr(lb), _iarr(ub)), "download")
         return out
+
+    def download_async(self, fid: int, out: np.ndarray, lb=None, ub=None) -> int:
+        """Queue a download of a 3-D field's box into `out` (Fortran-ordered float32 of
+        the box's shape, kept alive by the caller); returns the ticket for
+        download_wait.  The box is snapshotted in stream order, so steps queued after
+        this call do not change what arrives."""
+        dlb, dub = declared_extents(fid, self.im, self.jm, self.km)
+        lb = tuple(lb) if lb is not None else dlb
+        ub = tuple(ub) if ub is not None else dub
+        shape = tuple(ub[q] - lb[q] + 1 for q in range(3))
+        if out.shape != shape or out.dtype != np.float32 or not out.flags.f_contiguous:
+            raise ValueError(f"download_async: out must be Fortran-ordered float32 of shape {shape}")
+        t = C.c_longlong(-1)
+        self._check(self.lib.les_gpu_download_async(self._h, fid, _fptr(out), _iarr(lb), _iarr(ub), C.byref(t)),
+                    "download_async")
+        return t.value
+
+    def download_wait(self, ticket: int) -> None:
+        self._check(self.lib.les_gpu_download_wait(self._h, ticket), "download_wait")
 
     def commit(self):
         self._check(self.lib.les_gpu_commit_setup(self._h), "commit_setup")
