@@ -81,6 +81,20 @@ module module_LES_gpu
       real(c_float), intent(inout) :: host(*)
       integer(c_int), intent(in) :: lb(3), ub(3)
     end function
+    integer(c_int) function les_gpu_download_async(h, field, host, lb, ub, ticket) &
+        bind(C, name='les_gpu_download_async')
+      import :: c_int, c_ptr, c_float, c_long_long
+      type(c_ptr), value :: h
+      integer(c_int), value :: field
+      real(c_float), intent(inout) :: host(*)
+      integer(c_int), intent(in) :: lb(3), ub(3)
+      integer(c_long_long), intent(out) :: ticket
+    end function
+    integer(c_int) function les_gpu_download_wait(h, ticket) bind(C, name='les_gpu_download_wait')
+      import :: c_int, c_ptr, c_long_long
+      type(c_ptr), value :: h
+      integer(c_long_long), value :: ticket
+    end function
     integer(c_int) function les_gpu_commit_setup(h) bind(C, name='les_gpu_commit_setup')
       import :: c_int, c_ptr
       type(c_ptr), value :: h
