@@ -28,16 +28,6 @@
 
 namespace {
 
-// Thread blocks cover FX x FY x FZ cells (i, j, k); several k planes per block keep the
-// k-1/k+1 neighbours of the stencils inside one block's L1 working set.
-constexpr int FX = 32, FY = 2, FZ = 4;
-
-#define FUSED_IJK                                     \
-  const int i = blockIdx.x * FX + threadIdx.x + 1;    \
-  const int j = blockIdx.y * FY + threadIdx.y + 1;    \
-  const int k = blockIdx.z * FZ + threadIdx.z + 1;    \
-  if (i > d.im || j > d.jm || k > d.km) return;
-
 // Inputs the fused kernels only read go through the read-only (non-coherent) path:
 // u, v, w in velfg; sm, diu and the wall ratios in les.
 #define DIU_(n, i, j, k) __ldg(&d.diu[n][lix(d, (i), (j), (k))])
@@ -534,21 +524,60 @@ __device__ __forceinline__ float e8(const LesDom &d, int i, int j, int k) {
 __device__ __forceinline__ float e9(const LesDom &d, int i, int j, int k) { return (k > d.km) ? 0.f : DIU_(9, i, j, k); }
 
 // ------------------------------------------------------------------ les.f95:45-65
-__global__ void __launch_bounds__(FX *FY *FZ) k_les_sm3(LesDom d) {
-  FUSED_IJK
-  const float dudxx1 = e1(d, i, j, k);
-  const float dudyx1 = (e2(d, i - 1, j, k) + e2(d, i - 1, j + 1, k) + e2(d, i, j, k) + e2(d, i, j + 1, k)) * .25f;
-  const float dudzx1 = (e3(d, i - 1, j, k) + e3(d, i - 1, j, k + 1) + e3(d, i, j, k) + e3(d, i, j, k + 1)) * .25f;
-  const float dvdxx1 = (e4(d, i, j, k) + e4(d, i, j - 1, k) + e4(d, i + 1, j, k) + e4(d, i + 1, j - 1, k)) * .25f;
-  const float dvdyx1 = e5(d, i, j, k);
-  const float dvdzx1 = (e6(d, i, j - 1, k) + e6(d, i, j - 1, k + 1) + e6(d, i, j, k) + e6(d, i, j, k + 1)) * .25f;
-  const float dwdxx1 = (e7(d, i, j, k) + e7(d, i, j, k - 1) + e7(d, i + 1, j, k) + e7(d, i + 1, j, k - 1)) * .25f;
-  const float dwdyx1 = (e8(d, i, j, k) + e8(d, i, j, k - 1) + e8(d, i, j + 1, k) + e8(d, i, j + 1, k - 1)) * .25f;
-  const float dwdzx1 = e9(d, i, j, k);
-  const float cd = 0.1f * d.gr.delx1[k];
-  const float s1 = dudyx1 + dvdxx1, s2 = dwdyx1 + dvdzx1, s3 = dudzx1 + dwdxx1;
-  d.sm[lix(d, i, j, k)] =
-      cd * cd * __fsqrt_rn(2.f * (dudxx1 * dudxx1 + dvdyx1 * dvdyx1 + dwdzx1 * dwdzx1) + s1 * s1 + s2 * s2 + s3 * s3);
+// sm, as a k-march: a thread owns column (i, j) and walks a chunk of planes.  Of the 27
+// diu values a cell reads, the eight it shares with the plane above or below (e3, e6 at
+// k and k+1; e7, e8 at k-1 and k) are carried in registers, so a plane loads 19; the
+// next plane's 19 are requested before this plane's arithmetic.
+constexpr int STX = 32, STY = 8;
+
+struct SmPlane {  // the values of plane k+1 (k-faces) / k (in-plane) one step needs
+  float a3, b3, a6, b6;       // e3(i-1,j), e3(i,j), e6(i,j-1), e6(i,j) at the plane above
+  float a7, b7, a8, b8;       // e7(i,j), e7(i+1,j), e8(i,j), e8(i,j+1) at the plane itself
+  float e1, e5, e9;           // at the cell
+  float e2[4], e4[4];         // e2 at (i-1,j), (i-1,j+1), (i,j), (i,j+1); e4 at (i,j), (i,j-1), (i+1,j), (i+1,j-1)
+};
+
+__device__ __forceinline__ SmPlane sm_load(const LesDom &d, int i, int j, int k) {
+  SmPlane p;
+  p.a3 = e3(d, i - 1, j, k + 1); p.b3 = e3(d, i, j, k + 1);
+  p.a6 = e6(d, i, j - 1, k + 1); p.b6 = e6(d, i, j, k + 1);
+  p.a7 = e7(d, i, j, k); p.b7 = e7(d, i + 1, j, k);
+  p.a8 = e8(d, i, j, k); p.b8 = e8(d, i, j + 1, k);
+  p.e1 = e1(d, i, j, k); p.e5 = e5(d, i, j, k); p.e9 = e9(d, i, j, k);
+  p.e2[0] = e2(d, i - 1, j, k); p.e2[1] = e2(d, i - 1, j + 1, k); p.e2[2] = e2(d, i, j, k); p.e2[3] = e2(d, i, j + 1, k);
+  p.e4[0] = e4(d, i, j, k); p.e4[1] = e4(d, i, j - 1, k); p.e4[2] = e4(d, i + 1, j, k); p.e4[3] = e4(d, i + 1, j - 1, k);
+  return p;
+}
+
+__global__ void __launch_bounds__(STX *STY) k_les_sm3(LesDom d, int kchunk) {
+  const int i = blockIdx.x * STX + threadIdx.x + 1, j = blockIdx.y * STY + threadIdx.y + 1;
+  if (i > d.im || j > d.jm) return;
+  const int k0 = blockIdx.z * kchunk + 1, k1 = min(k0 + kchunk - 1, d.km);
+  // carried: e3, e6 at plane k (a3c, b3c, a6c, b6c) and e7, e8 at plane k-1
+  float a3c = e3(d, i - 1, j, k0), b3c = e3(d, i, j, k0), a6c = e6(d, i, j - 1, k0), b6c = e6(d, i, j, k0);
+  float a7m = e7(d, i, j, k0 - 1), b7m = e7(d, i + 1, j, k0 - 1), a8m = e8(d, i, j, k0 - 1),
+        b8m = e8(d, i, j + 1, k0 - 1);
+  SmPlane cur = sm_load(d, i, j, k0);
+  for (int k = k0; k <= k1; ++k) {
+    SmPlane nxt = cur;
+    if (k < k1) nxt = sm_load(d, i, j, k + 1);
+    const float dudxx1 = cur.e1;
+    const float dudyx1 = (cur.e2[0] + cur.e2[1] + cur.e2[2] + cur.e2[3]) * .25f;
+    const float dudzx1 = (a3c + cur.a3 + b3c + cur.b3) * .25f;
+    const float dvdxx1 = (cur.e4[0] + cur.e4[1] + cur.e4[2] + cur.e4[3]) * .25f;
+    const float dvdyx1 = cur.e5;
+    const float dvdzx1 = (a6c + cur.a6 + b6c + cur.b6) * .25f;
+    const float dwdxx1 = (cur.a7 + a7m + cur.b7 + b7m) * .25f;
+    const float dwdyx1 = (cur.a8 + a8m + cur.b8 + b8m) * .25f;
+    const float dwdzx1 = cur.e9;
+    const float cd = 0.1f * d.gr.delx1[k];
+    const float s1 = dudyx1 + dvdxx1, s2 = dwdyx1 + dvdzx1, s3 = dudzx1 + dwdxx1;
+    d.sm[lix(d, i, j, k)] =
+        cd * cd * __fsqrt_rn(2.f * (dudxx1 * dudxx1 + dvdyx1 * dvdyx1 + dwdzx1 * dwdzx1) + s1 * s1 + s2 * s2 + s3 * s3);
+    a3c = cur.a3; b3c = cur.b3; a6c = cur.a6; b6c = cur.b6;
+    a7m = cur.a7; b7m = cur.b7; a8m = cur.a8; b8m = cur.b8;
+    cur = nxt;
+  }
 }
 
 // ------------------------------------------------------------------ les.f95:83-242
@@ -906,7 +935,6 @@ __global__ void __launch_bounds__(VTX *VTY) k_les_visc_fix(LesDom d, uint3 g) {
   });
 }
 
-inline dim3 fgrid(const LesDom &d) { return dim3((d.im + FX - 1) / FX, (d.jm + FY - 1) / FY, (d.km + FZ - 1) / FZ); }
 
 }  // namespace
 
@@ -979,8 +1007,14 @@ void les_launch_velfg_fused(const LesDom &d, bool with_feedbf, LesCtx ctx) {
 }
 
 void les_launch_les_fused(const LesDom &d, bool with_adam, LesCtx ctx) {
-  const dim3 g = fgrid(d), b(FX, FY, FZ);
-  LAUNCH(ctx, k_les_sm3<<<g, b, 0, ctx.s>>>(d));
+  {  // sm: chunks of planes enough for about sixteen blocks per SM, 8 to 32 planes each
+    const long long tiles = (long long)((d.im + STX - 1) / STX) * ((d.jm + STY - 1) / STY);
+    const int sms = d.sms > 0 ? d.sms : 152;
+    const int nch = (int)std::max<long long>(1, (16LL * sms + tiles - 1) / tiles);
+    const int kc = std::min(d.km, std::max(8, std::min(32, (d.km + nch - 1) / nch)));
+    const dim3 g((d.im + STX - 1) / STX, (d.jm + STY - 1) / STY, (d.km + kc - 1) / kc);
+    LAUNCH(ctx, k_les_sm3<<<g, dim3(STX, STY), 0, ctx.s>>>(d, kc));
+  }
   les_launch_boundsm(d, ctx);
   // the k-march: 32 x 8 column tiles, chunks of VKC planes
   const dim3 gv((d.im + VTX - 1) / VTX, (d.jm + VTY - 1) / VTY, (d.km + VKC - 1) / VKC);
