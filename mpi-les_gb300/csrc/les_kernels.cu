@@ -229,17 +229,33 @@ __global__ void k_bondfg(LesDom d) {
 
 // ------------------------------------------------------------------ press.f95:49-60
 // (u, v, w, f, g, h are only read here: read-only loads)
+// The values one cell reads: u(i-1), u, v(j-1), v, w(k-1), w, f(i-1), f, g(j-1), g,
+// h(k-1), h at (i, j, k).
+struct RhsIn {
+  float um, uc, vm, vc, wm, wc, fm, fc, gm, gc, hm, hc;
+};
+__device__ __forceinline__ RhsIn rhs_load(const LesDom &d, int c) {
+  RhsIn x;
+  x.um = __ldg(d.u + c - 1); x.uc = __ldg(d.u + c);
+  x.vm = __ldg(d.v + c - d.pi); x.vc = __ldg(d.v + c);
+  x.wm = __ldg(d.w + c - d.np); x.wc = __ldg(d.w + c);
+  x.fm = __ldg(d.f + c - 1); x.fc = __ldg(d.f + c);
+  x.gm = __ldg(d.g + c - d.pi); x.gc = __ldg(d.g + c);
+  x.hm = __ldg(d.h + c - d.np); x.hc = __ldg(d.h + c);
+  return x;
+}
 template <bool P2, bool ZF>
-__device__ __forceinline__ float rhs_cell(const LesDom &d, int i, int j, int k, int c, unsigned &bd) {
+__device__ __forceinline__ float rhs_comp(const LesDom &d, int i, int j, int k, const RhsIn &x, unsigned &bd) {
   const float *dx1 = d.gr.dx1, *dy1 = d.gr.dy1, *dzn = d.gr.dzn;
   const float rx = d.gr.rdx1[i], ry = d.gr.rdy1[j], rz = d.gr.rdzn[k];
-  const float *u = d.u, *v = d.v, *w = d.w, *f = d.f, *g = d.g, *h = d.h;
-  const float r = dvs<P2, ZF>(-__ldg(u + c - 1) + __ldg(u + c), dx1[i], rx, bd) +
-                  dvs<P2, ZF>(-__ldg(v + c - d.pi) + __ldg(v + c), dy1[j], ry, bd) +
-                  dvz<ZF>(-__ldg(w + c - d.np) + __ldg(w + c), dzn[k], rz, bd);
-  return dvs<P2, ZF>(__ldg(f + c) - __ldg(f + c - 1), dx1[i], rx, bd) +
-         dvs<P2, ZF>(__ldg(g + c) - __ldg(g + c - d.pi), dy1[j], ry, bd) +
-         dvz<ZF>(__ldg(h + c) - __ldg(h + c - d.np), dzn[k], rz, bd) + dvz<ZF>(r, d.dt, d.rdt, bd);
+  const float r = dvs<P2, ZF>(-x.um + x.uc, dx1[i], rx, bd) + dvs<P2, ZF>(-x.vm + x.vc, dy1[j], ry, bd) +
+                  dvz<ZF>(-x.wm + x.wc, dzn[k], rz, bd);
+  return dvs<P2, ZF>(x.fc - x.fm, dx1[i], rx, bd) + dvs<P2, ZF>(x.gc - x.gm, dy1[j], ry, bd) +
+         dvz<ZF>(x.hc - x.hm, dzn[k], rz, bd) + dvz<ZF>(r, d.dt, d.rdt, bd);
+}
+template <bool P2, bool ZF>
+__device__ __forceinline__ float rhs_cell(const LesDom &d, int i, int j, int k, int c, unsigned &bd) {
+  return rhs_comp<P2, ZF>(d, i, j, k, rhs_load(d, c), bd);
 }
 // Compensated running sum of FP32 terms: hi by TwoSum, lo gathers the rounding errors.
 struct PairSum {
@@ -291,21 +307,32 @@ __device__ __forceinline__ void rhs_block(const LesDom &d, float *dst, int ghost
   const int i = min(i0, d.im), j = min(j0, d.jm);  // past the edge: the edge cell again, not stored
   const int ka = bz * RKC + 1, kb = min(ka + RKC - 1, d.km);
   const float axy = d.gr.dx1[i] * d.gr.dy1[j];
+  // periodic ghost copies of this row: 1 -> jm+1, 2 -> jm+2, jm-1 -> -1, jm -> 0
+  // (offsets from the row's own cell; 0 = none; jm = 2 gives two copies per row)
+  int go1 = 0, go2 = 0;
+  if (ghost) {
+    if (j == 1) go1 = d.jm * d.pi;
+    if (j == 2) go1 = d.jm * d.pi;
+    if (j == d.jm - 1) go2 = -d.jm * d.pi;
+    if (j == d.jm) go2 = -d.jm * d.pi;
+  }
   unsigned bd = 0;
   PairSum acc;
+  // the loads of plane k+1 are issued before plane k's arithmetic
+  int c = lix(d, i, j, ka);
+  RhsIn cur = rhs_load(d, c);
   for (int k = ka; k <= kb; ++k) {
-    const int c = lix(d, i, j, k);
-    const float rr = rhs_cell<P2, ZF>(d, i, j, k, c, bd);
+    RhsIn nxt = cur;
+    if (k < kb) nxt = rhs_load(d, c + d.np);
+    const float rr = rhs_comp<P2, ZF>(d, i, j, k, cur, bd);
     if (in) {
       dst[c] = rr;
-      if (ghost) {
-        if (j == 1) dst[lix(d, i, d.jm + 1, k)] = rr;
-        if (j == 2) dst[lix(d, i, d.jm + 2, k)] = rr;
-        if (j == d.jm - 1) dst[lix(d, i, -1, k)] = rr;
-        if (j == d.jm) dst[lix(d, i, 0, k)] = rr;
-      }
+      if (go1) dst[c + go1] = rr;
+      if (go2) dst[c + go2] = rr;
       acc.add(axy * d.gr.dzn[k] * rr);
     }
+    cur = nxt;
+    c += d.np;
   }
   if (ZF && defer_block(bd, d.fix[FIX_RHS])) return;
   block_part(d, acc, (int)((bz * g.y + by) * g.x + bx));
@@ -363,11 +390,26 @@ __global__ void __launch_bounds__(FIN_THREADS) k_finish_mean(LesDom d, int npart
     d.cnt[8] = 0u;
   }
 }
-__global__ void __launch_bounds__(BX *BY) k_sub_mean(LesDom d, float *a, int slot) {
-  INTERIOR_IJK
-  const int c = lix(d, i, j, k);
-  a[c] = a[c] - d.fscal[slot];
+// a -= mean over the interior: one warp per row (j, k), float4 columns (interior rows
+// start 16-byte aligned), the ragged end of a row one float at a time
+constexpr int SUB_ROWS = 8;
+__global__ void __launch_bounds__(32 * SUB_ROWS) k_sub_mean(LesDom d, float *a, int slot) {
+  const int row = blockIdx.x * SUB_ROWS + (int)(threadIdx.x >> 5);  // (j-1) + jm*(k-1)
+  if (row >= d.jm * d.km) return;
+  const int lane = threadIdx.x & 31;
+  const int j = row % d.jm + 1, k = row / d.jm + 1;
+  float *r = a + lix(d, 1, j, k);
+  const float m = d.fscal[slot];
+  const int nq = d.im >> 2;
+  float4 *r4 = reinterpret_cast<float4 *>(r);
+  for (int q = lane; q < nq; q += 32) {
+    float4 v = r4[q];
+    v.x = v.x - m; v.y = v.y - m; v.z = v.z - m; v.w = v.w - m;
+    r4[q] = v;
+  }
+  for (int i = 4 * nq + lane; i < d.im; i += 32) r[i] = r[i] - m;
 }
+inline unsigned sub_mean_blocks(const LesDom &d) { return (unsigned)((d.jm * d.km + SUB_ROWS - 1) / SUB_ROWS); }
 
 // ------------------------------------------------------------------ press.f95:89-122
 __global__ void k_sor_begin(LesDom d) {
@@ -556,7 +598,7 @@ int les_interior_blocks(const LesDom &d) {
 
 void les_launch_rhs_mean(const LesDom &d, LesCtx ctx) {
   launch_rhs(d, d.rhs, 0, ctx);
-  LAUNCH(ctx, k_sub_mean<<<interior_grid(d, d.km), dim3(BX, BY), 0, ctx.s>>>(d, d.rhs, SC_RHSAV));
+  LAUNCH(ctx, k_sub_mean<<<sub_mean_blocks(d), 32 * SUB_ROWS, 0, ctx.s>>>(d, d.rhs, SC_RHSAV));
 }
 
 void les_launch_rhs_sor(const LesDom &d, LesCtx ctx) { launch_rhs(d, d.sorR, 1, ctx); }
@@ -595,7 +637,7 @@ void les_launch_pav_adjust(const LesDom &d, LesCtx ctx) {
   const int nb = (int)(gr.x * gr.y * gr.z);
   LAUNCH(ctx, k_pav_part<<<gr, dim3(BX, BY), 0, ctx.s>>>(d));
   LAUNCH(ctx, k_finish_mean<<<FIN_BLOCKS, FIN_THREADS, 0, ctx.s>>>(d, nb, SC_PAV));
-  LAUNCH(ctx, k_sub_mean<<<interior_grid(d, d.km), dim3(BX, BY), 0, ctx.s>>>(d, d.p, SC_PAV));
+  LAUNCH(ctx, k_sub_mean<<<sub_mean_blocks(d), 32 * SUB_ROWS, 0, ctx.s>>>(d, d.p, SC_PAV));
   les_launch_boundp1(d, ctx, 0);
   les_launch_boundp2(d, ctx, 0);
 }
