@@ -74,6 +74,33 @@ __device__ __forceinline__ float relax_pair(int q, float4 &cur, float pl, float 
   return part;
 }
 
+// relax_pair for the TMA march: the squared corrections of the relaxed elements are
+// weighted by m[e] (1 for the cells this thread owns, 0 for ring and outside cells:
+// multiplies, which the FP pipe has room for, instead of selects).
+__device__ __forceinline__ float relax_pair_m(int q, float4 &cur, float pl, float pr, const float4 &pn,
+                                              const float4 &pso, const float4 &pu, const float4 &pdn,
+                                              const float4 &rr, float rhsav, float omega, float cn1,
+                                              const float (&c2l)[4], const float (&c2s)[4], float c3l, float c3s,
+                                              float c4l, float c4s, bool west0, int east_e, const float (&m)[4]) {
+  const float4 c = cur;
+  if (q == 0) {
+    const float ra = relax_e<0>(c, pl, pr, pn, pso, pu, pdn, rr, rhsav, omega, cn1, c2l, c2s, c3l, c3s, c4l, c4s,
+                                west0, east_e == 0);
+    const float rb = relax_e<2>(c, pl, pr, pn, pso, pu, pdn, rr, rhsav, omega, cn1, c2l, c2s, c3l, c3s, c4l, c4s,
+                                false, east_e == 2);
+    cur.x = c.x + ra;
+    cur.z = c.z + rb;
+    return ra * ra * m[0] + rb * rb * m[2];
+  }
+  const float ra = relax_e<1>(c, pl, pr, pn, pso, pu, pdn, rr, rhsav, omega, cn1, c2l, c2s, c3l, c3s, c4l, c4s,
+                              false, east_e == 1);
+  const float rb = relax_e<3>(c, pl, pr, pn, pso, pu, pdn, rr, rhsav, omega, cn1, c2l, c2s, c3l, c3s, c4l, c4s,
+                              false, east_e == 3);
+  cur.y = c.y + ra;
+  cur.w = c.w + rb;
+  return ra * ra * m[1] + rb * rb * m[3];
+}
+
 // Per-thread geometry shared by both kernels.
 constexpr int NO_GHOST = -1000;
 struct Lane {
@@ -516,6 +543,15 @@ __global__ void __launch_bounds__(NX *NY, min_ctas(NX))
   int st0 = (s_begin - mfirst) % D, st1 = (s_begin + 1 - mfirst) % D;
   uint32_t ph1 = (uint32_t)(((s_begin + 1 - mfirst) / D) & 1);
 
+  // residual weights: red counts the owned cells of the tile, black runs on owned
+  // threads only
+  float mred[4], mblack[4];
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    mblack[e] = L.ival[e] ? 1.f : 0.f;
+    mred[e] = (L.owned && L.ival[e]) ? 1.f : 0.f;
+  }
+
   auto step = [&](auto UC, int s) {
     constexpr int U = decltype(UC)::value;  // s = U modulo 4
     constexpr int S0 = U, SP1 = (U + 1) % 4, SM1 = (U + 3) % 4, SM2 = (U + 2) % 4;
@@ -545,9 +581,9 @@ __global__ void __launch_bounds__(NX *NY, min_ctas(NX))
       if (L.row_red) {
         R[C0] = S.rhs[st0][r][c4];
         const float4 pn = S.p[st0][r + 1][c4], pso = S.p[st0][r - 1][c4];
-        part += relax_pair(q, P[S0], rpl, rpr, pn, pso, P[SP1], P[SM1], R[C0], rhsav, omega, CK[C0], c2l, c2s, c3l,
-                           c3s, C4L[C0], C4S[C0], L.west0, L.east_e, L.owned && (!KC || (s >= ka && s <= kb)),
-                           L.ival);
+        const float pr_ = relax_pair_m(q, P[S0], rpl, rpr, pn, pso, P[SP1], P[SM1], R[C0], rhsav, omega, CK[C0], c2l,
+                                       c2s, c3l, c3s, C4L[C0], C4S[C0], L.west0, L.east_e, mred);
+        if (!KC || (s >= ka && s <= kb)) part += pr_;
       }
     }
     S.red[U & 1][r][c4] = P[S0];
@@ -555,8 +591,8 @@ __global__ void __launch_bounds__(NX *NY, min_ctas(NX))
     if ((KC ? (s - 1 >= ka && s - 1 <= kb) : (s >= 2)) && L.owned) {
       const int k = s - 1;
       const float4 pn = S.red[(U + 1) & 1][r + 1][c4], pso = S.red[(U + 1) & 1][r - 1][c4];
-      part += relax_pair(q, P[SM1], bpl, bpr, pn, pso, P[S0], P[SM2], R[CM], rhsav, omega, CK[CM], c2l, c2s, c3l,
-                         c3s, C4L[CM], C4S[CM], L.west0, L.east_e, true, L.ival);
+      part += relax_pair_m(q, P[SM1], bpl, bpr, pn, pso, P[S0], P[SM2], R[CM], rhsav, omega, CK[CM], c2l, c2s, c3l,
+                           c3s, C4L[CM], C4S[CM], L.west0, L.east_e, mblack);
       store_final(d, a, L, k, P[SM1]);
     }
     {  // Kahan accumulation of this step's squared corrections
