@@ -90,7 +90,7 @@ struct les_handle {
   float *sor_d[3] = {};           // internal buffers of the fused SOR sweep (A, B, rhs)
   float *diu_d[10] = {};          // diu1..9 stored by velfg for les ([0] unused)
   float *rsp_d = nullptr;         // two planes: u/uspd and v/vspd at k = 1
-  unsigned int *cnt_d = nullptr;  // CTA tickets (fused SOR sweep, finish_mean)
+  unsigned int *cnt_d = nullptr;  // CTA tickets (fused SOR sweep, finish_mean, uout)
   int *fix_d = nullptr;           // deferred-block lists (FIX_COUNT lists of fix_len ints)
   size_t fix_len = 0;
   int sms = 0;

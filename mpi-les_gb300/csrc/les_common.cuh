@@ -71,7 +71,7 @@ struct LesDom {
   float *fscal;    // float copies of uout/rhsav/pav for kernels
   float *sorA, *sorB;  // ping-pong p buffers of the fused SOR sweep (with periodic ghost rows)
   float *sorR;         // rhs of the fused SOR sweep (with periodic ghost rows)
-  unsigned int *cnt;  // CTA completion tickets: [0] fused SOR sweep, [8] finish_mean
+  unsigned int *cnt;  // CTA completion tickets: [0] fused SOR sweep, [8] finish_mean, [12] bondv1 uout
   double *part2;      // second-level partial sums of finish_mean (FIN_BLOCKS)
   int sms;         // SMs of the device (grid sizing)
   // xy_pow2: every x and y spacing is the same power of two (dvs multiplies);

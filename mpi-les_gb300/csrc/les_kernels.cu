@@ -96,12 +96,17 @@ __global__ void __launch_bounds__(BX *BY) k_bondv1_fill(LesDom d) {
   const int x = lix(d, i, j, k), x1 = lix(d, 1, j, k);
   d.u[x] = d.u[x1]; d.v[x] = d.v[x1]; d.w[x] = d.w[x1];
 }
-// uout = (max(0, max u(im)) + min(0, min u(im)))/2 (bondv1.f95:171-187); one block.
-__global__ void __launch_bounds__(1024) k_bondv1_uout(LesDom d) {
-  __shared__ float smax[32], smin[32];
+// uout = (max(0, max u(im)) + min(0, min u(im)))/2 (bondv1.f95:171-187).  The values
+// u(im, j, k) are one per row, so many blocks gather them; each block's max and min go
+// to part[], and the last block to finish combines them (max and min are exact in any
+// order).
+constexpr int UOUT_BLOCKS = 64, UOUT_THREADS = 256;
+__global__ void __launch_bounds__(UOUT_THREADS) k_bondv1_uout(LesDom d) {
+  __shared__ float smax[UOUT_THREADS / 32], smin[UOUT_THREADS / 32];
+  __shared__ int last;
   float aaa = 0.f, bbb = 0.f;
   const int n = d.jm * d.km;
-  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+  for (int q = blockIdx.x * UOUT_THREADS + threadIdx.x; q < n; q += gridDim.x * UOUT_THREADS) {
     const int j = q % d.jm + 1, k = q / d.jm + 1;
     const float x = U_(d.im, j, k);
     aaa = fmaxf(aaa, x);
@@ -115,11 +120,24 @@ __global__ void __launch_bounds__(1024) k_bondv1_uout(LesDom d) {
   __syncthreads();
   if (threadIdx.x == 0) {
     float a = 0.f, b = 0.f;
-    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) { a = fmaxf(a, smax[q]); b = fminf(b, smin[q]); }
-    const float uout = (a + b) / 2.f;
-    d.fscal[SC_UOUT] = uout;
-    d.scal[SC_UOUT] = (double)uout;
+    for (int q = 0; q < UOUT_THREADS / 32; ++q) { a = fmaxf(a, smax[q]); b = fminf(b, smin[q]); }
+    d.part[2 * blockIdx.x] = (double)a;
+    d.part[2 * blockIdx.x + 1] = (double)b;
+    __threadfence();
+    last = (atomicAdd(d.cnt + 12, 1u) == gridDim.x - 1);
   }
+  __syncthreads();
+  if (!last || threadIdx.x != 0) return;
+  __threadfence();
+  float a = 0.f, b = 0.f;
+  for (int q = 0; q < (int)gridDim.x; ++q) {
+    a = fmaxf(a, (float)((volatile double *)d.part)[2 * q]);
+    b = fminf(b, (float)((volatile double *)d.part)[2 * q + 1]);
+  }
+  const float uout = (a + b) / 2.f;
+  d.fscal[SC_UOUT] = uout;
+  d.scal[SC_UOUT] = (double)uout;
+  d.cnt[12] = 0u;
 }
 // advective outflow (bondv1.f95:191-207)
 __global__ void k_bondv1_outflow(LesDom d) {
@@ -556,7 +574,7 @@ void les_launch_bondv1(const LesDom &d, int n, LesCtx ctx) {
   if (n == 1) {
     LAUNCH(ctx, k_bondv1_fill<<<dim3((d.im - 1 + BX - 1) / BX, (d.jm + BY - 1) / BY, d.km), dim3(BX, BY), 0, ctx.s>>>(d));
   }
-  LAUNCH(ctx, k_bondv1_uout<<<1, 1024, 0, ctx.s>>>(d));
+  LAUNCH(ctx, k_bondv1_uout<<<UOUT_BLOCKS, UOUT_THREADS, 0, ctx.s>>>(d));
   LAUNCH(ctx, k_bondv1_outflow<<<dim3((d.jm + 127) / 128, d.km), 128, 0, ctx.s>>>(d));
   LAUNCH(ctx, k_bondv1_periodic<<<dim3((d.im + 2 + 127) / 128, d.km + 2), 128, 0, ctx.s>>>(d));
   LAUNCH(ctx, k_bondv1_topbottom<<<dim3((d.im + 2 + 127) / 128, d.jm + 3), 128, 0, ctx.s>>>(d));
