@@ -1,15 +1,20 @@
 // les_sor16.cu -- the fused SOR sweep (les_sor.cu) on 16-column tiles: 56 interior i
-// cells per CTA, two CTAs per SM.  Used for domains that share the GPU, whose SOR
-// march is never split in k, with a uniform cn1 (the only form the register kernel is
-// instantiated for here).
+// cells per CTA, two CTAs per SM, for narrow domains (batch members, and small domains
+// alone when the tuner finds them faster), whole march or k chunks, with a uniform cn1
+// (the only form the register kernel is instantiated for here).
 #include "les_sor_kern.cuh"
 
 namespace {
 
+template <int NY, int D, bool KC>
+void launch16_kc(const LesDom &d, const SorArgs &a, const CUtensorMap *tp, const CUtensorMap *tr, cudaStream_t s) {
+  if (tp && tr) launch_tma_kc<16, NY, D, KC>(d, a, *tp, *tr, s);
+  else launch_reg_kc<16, NY, KC>(d, a, 0, s);
+}
 template <int NY, int D>
 void launch16(const LesDom &d, const SorArgs &a, const CUtensorMap *tp, const CUtensorMap *tr, cudaStream_t s) {
-  if (tp && tr) launch_tma_kc<16, NY, D, false>(d, a, *tp, *tr, s);
-  else launch_reg_kc<16, NY, false>(d, a, 0, s);
+  if (a.nchunk > 1) launch16_kc<NY, D, true>(d, a, tp, tr, s);
+  else launch16_kc<NY, D, false>(d, a, tp, tr, s);
 }
 
 }  // namespace

@@ -65,10 +65,11 @@ static void plan_pick(const LesDom &d, LesStepPlan *plan) {
     if (plan->fixed.nx && (plan->fixed.nx == 32 || d.gr.cn1k)) sh.nx = plan->fixed.nx;
     if (plan->fixed.ny) sh.ny = plan->fixed.ny;
     const int tiles = les_sor_fused_tiles(d.im, d.jm, sh);
-    // 16-column tiles march the whole k range (no k-chunk kernels are built for them)
+    // k chunks: fixed by the caller, else tuned for the class, else (alone on the GPU,
+    // 32-column tiles) enough to fill the SMs
     int kc = d.km;
-    if (sh.nx == 32 && plan->fixed.kchunk > 0) kc = plan->fixed.kchunk;
-    else if (sh.nx == 32 && sh.kchunk > 0 && !plan->fixed.nx && !plan->fixed.ny) kc = sh.kchunk;  // tuned
+    if (plan->fixed.kchunk > 0) kc = plan->fixed.kchunk;
+    else if (sh.kchunk > 0 && !plan->fixed.nx && !plan->fixed.ny) kc = sh.kchunk;  // tuned
     else if (sh.nx == 32 && !d.sor_ksplit) kc = les_sor_pick_kchunk(tiles, d.km, d.sms > 0 ? d.sms : 152);
     kc = kc < 1 ? 1 : (kc > d.km ? d.km : kc);
     if (plan->part_cap > 0 && (long long)tiles * ((d.km + kc - 1) / kc) > plan->part_cap) kc = d.km;

@@ -42,23 +42,25 @@ int sms_of(const LesDom &d) { return d.sms > 0 ? d.sms : 152; }
 std::vector<SorShape> candidates(const LesDom &d, bool shared) {
   std::vector<SorShape> c;
   const int sms = sms_of(d);
-  for (int ny : {16, 20, 24, 28}) {
-    c.push_back(SorShape{16, ny, d.km});
-    if (shared) {
-      c.push_back(SorShape{32, ny, d.km});
-      continue;
+  for (int ny : {16, 20, 24, 28})
+    for (int nx : {32, 16}) {
+      if (shared) {
+        c.push_back(SorShape{nx, ny, d.km});
+        continue;
+      }
+      // alone: the whole march and k splits up to two waves of CTAs (a 32-column CTA
+      // holds an SM, two 16-column ones share one), chunks of >= 4 planes
+      const int tiles = les_sor_fused_tiles(d.im, d.jm, SorShape{nx, ny, 0});
+      const long long slots = (nx == 16 ? 2LL : 1LL) * sms;
+      int last = -1;
+      for (int nch : {1, 2, 3, 4, 6, 8, 12, 16, 24}) {
+        const int kc = (d.km + nch - 1) / nch;
+        const int n = (d.km + kc - 1) / kc;
+        if (kc == last || (nch > 1 && (kc < 4 || (long long)tiles * n > 2LL * slots))) continue;
+        c.push_back(SorShape{nx, ny, kc});
+        last = kc;
+      }
     }
-    // alone: the whole march and k splits up to two waves of CTAs, chunks of >= 4 planes
-    const int tiles = les_sor_fused_tiles(d.im, d.jm, SorShape{32, ny, 0});
-    int last = -1;
-    for (int nch : {1, 2, 3, 4, 6, 8, 12, 16, 24}) {
-      const int kc = (d.km + nch - 1) / nch;
-      const int n = (d.km + kc - 1) / kc;
-      if (kc == last || (nch > 1 && (kc < 4 || (long long)tiles * n > 2LL * sms))) continue;
-      c.push_back(SorShape{32, ny, kc});
-      last = kc;
-    }
-  }
   return c;
 }
 
