@@ -27,6 +27,16 @@
 
 namespace {
 
+// The fast build (-fopenmp -DLES_REF_PAR, the timed CPU baseline) runs the stencil
+// loops over k planes on all host threads: each cell of such a loop depends only on
+// other arrays or on cells of the other SOR colour, so the fields are unchanged.  Only
+// the SOR residual is summed differently there (per-plane partials, in plane order).
+#if defined(_OPENMP) && defined(LES_REF_PAR)
+#define LES_REF_OMP_FOR _Pragma("omp parallel for schedule(static)")
+#else
+#define LES_REF_OMP_FOR
+#endif
+
 thread_local std::string g_err;
 
 struct RefError {
@@ -233,18 +243,21 @@ struct Ref {
 
   // ---------------------------------------------------------------- velnw.f95:27-59
   void velnw() {
+    LES_REF_OMP_FOR
     for (int k = 1; k <= km; ++k)
       for (int j = 1; j <= jm; ++j)
         for (int i = 1; i <= im; ++i) {
           const T pz = (-p(i, j, k) + p(i + 1, j, k)) / ro / dxs(i);
           u(i, j, k) = u(i, j, k) + dt * (f(i, j, k) - pz);
         }
+    LES_REF_OMP_FOR
     for (int k = 1; k <= km; ++k)
       for (int j = 1; j <= jm; ++j)
         for (int i = 1; i <= im; ++i) {
           const T pz = (-p(i, j, k) + p(i, j + 1, k)) / ro / dys(j);
           v(i, j, k) = v(i, j, k) + dt * (g(i, j, k) - pz);
         }
+    LES_REF_OMP_FOR
     for (int k = 1; k <= km - 1; ++k)
       for (int j = 1; j <= jm; ++j)
         for (int i = 1; i <= im; ++i) {
@@ -353,6 +366,7 @@ struct Ref {
         vspd(i, j) = pow_half(a * a + b * b, sqrt_half);
       }
     // vel2.f95:74-89
+    LES_REF_OMP_FOR
     for (int k = 1; k <= km; ++k)
       for (int j = 1; j <= jm; ++j)
         for (int i = 1; i <= im; ++i) {
@@ -367,6 +381,7 @@ struct Ref {
           cov9(i, j, k) = nou9(i, j, k) * diu9(i, j, k);
         }
     // vel2.f95:103-111
+    LES_REF_OMP_FOR
     for (int k = 1; k <= km; ++k)
       for (int j = 1; j <= jm; ++j)
         for (int i = 1; i <= im; ++i) {
@@ -375,6 +390,7 @@ struct Ref {
           cov2(i, j, k) = nou2(i, j, k) * diu2(i, j, k);
         }
     // vel2.f95:119-127
+    LES_REF_OMP_FOR
     for (int k = 2; k <= km + 1; ++k)
       for (int j = 1; j <= jm; ++j)
         for (int i = 1; i <= im; ++i) {
@@ -391,6 +407,7 @@ struct Ref {
         cov3(i, j, 1) = nou3(i, j, 1) * diu3(i, j, 1);
       }
     // vel2.f95:144-152
+    LES_REF_OMP_FOR
     for (int k = 1; k <= km; ++k)
       for (int j = 1; j <= jm; ++j)
         for (int i = 1; i <= im; ++i) {
@@ -399,6 +416,7 @@ struct Ref {
           cov4(i, j, k) = (nou4(i, j, k) - u0) * diu4(i, j, k);
         }
     // vel2.f95:154-162
+    LES_REF_OMP_FOR
     for (int k = 2; k <= km + 1; ++k)
       for (int j = 1; j <= jm; ++j)
         for (int i = 1; i <= im; ++i) {
@@ -415,6 +433,7 @@ struct Ref {
         cov6(i, j, 1) = nou6(i, j, 1) * diu6(i, j, 1);
       }
     // vel2.f95:179-187
+    LES_REF_OMP_FOR
     for (int k = 1; k <= km - 1; ++k)
       for (int j = 1; j <= jm; ++j)
         for (int i = 1; i <= im; ++i) {
@@ -423,6 +442,7 @@ struct Ref {
           cov7(i, j, k) = (nou7(i, j, k) - u0) * diu7(i, j, k);
         }
     // vel2.f95:189-197
+    LES_REF_OMP_FOR
     for (int k = 1; k <= km - 1; ++k)
       for (int j = 1; j <= jm; ++j)
         for (int i = 1; i <= im; ++i) {
@@ -431,12 +451,14 @@ struct Ref {
           cov8(i, j, k) = nou8(i, j, k) * diu8(i, j, k);
         }
     // halo copies (vel2.f95:202-318), non-MPI branches
+    LES_REF_OMP_FOR
     for (int k = 1; k <= km; ++k)
       for (int j = 1; j <= jm; ++j) {
         nou1(im + 1, j, k) = nou1(im, j, k);
         diu1(im + 1, j, k) = diu1(im, j, k);
         cov1(im + 1, j, k) = cov1(im, j, k);
       }
+    LES_REF_OMP_FOR
     for (int k = 1; k <= km; ++k)
       for (int i = 1; i <= im; ++i) {
         nou2(i, 0, k) = nou2(i, jm, k);
@@ -446,12 +468,14 @@ struct Ref {
         diu2(i, jm + 1, k) = diu2(i, 1, k);
         cov2(i, jm + 1, k) = cov2(i, 1, k);
       }
+    LES_REF_OMP_FOR
     for (int k = 1; k <= km; ++k)
       for (int j = 1; j <= jm; ++j) {
         nou4(im + 1, j, k) = nou4(im, j, k);
         diu4(im + 1, j, k) = diu4(im, j, k);
         cov4(im + 1, j, k) = cov4(im, j, k);
       }
+    LES_REF_OMP_FOR
     for (int k = 1; k <= km; ++k)
       for (int i = 1; i <= im; ++i) {
         nou5(i, 0, k) = nou5(i, jm, k);
@@ -461,12 +485,14 @@ struct Ref {
         diu5(i, jm + 1, k) = diu5(i, 1, k);
         cov5(i, jm + 1, k) = cov5(i, 1, k);
       }
+    LES_REF_OMP_FOR
     for (int k = 1; k <= km - 1; ++k)
       for (int j = 1; j <= jm; ++j) {
         nou7(im + 1, j, k) = nou7(im, j, k);
         diu7(im + 1, j, k) = diu7(im, j, k);
         cov7(im + 1, j, k) = cov7(im, j, k);
       }
+    LES_REF_OMP_FOR
     for (int k = 1; k <= km - 1; ++k)
       for (int i = 1; i <= im; ++i) {
         nou8(i, 0, k) = nou8(i, jm, k);
@@ -476,11 +502,13 @@ struct Ref {
         diu8(i, jm + 1, k) = diu8(i, 1, k);
         cov8(i, jm + 1, k) = cov8(i, 1, k);
       }
+    LES_REF_OMP_FOR
     for (int k = 1; k <= km + 1; ++k)
       for (int j = 1; j <= jm + 1; ++j) {
         diu2(im + 1, j, k) = diu2(im, j, k);
         diu3(im + 1, j, k) = diu3(im, j, k);
       }
+    LES_REF_OMP_FOR
     for (int k = 1; k <= km + 1; ++k)
       for (int i = 1; i <= im + 1; ++i) {
         diu4(i, 0, k) = diu4(i, jm, k);
@@ -501,6 +529,7 @@ struct Ref {
           &cov6 = cov[6], &cov7 = cov[7], &cov8 = cov[8], &cov9 = cov[9];
     FA<T> &diu1 = diu[1], &diu2 = diu[2], &diu3 = diu[3], &diu4 = diu[4], &diu5 = diu[5],
           &diu6 = diu[6], &diu7 = diu[7], &diu8 = diu[8], &diu9 = diu[9];
+    LES_REF_OMP_FOR
     for (int k = 1; k <= km; ++k)
       for (int j = 1; j <= jm; ++j)
         for (int i = 1; i <= im; ++i) {
@@ -514,6 +543,7 @@ struct Ref {
           const T df = vn * dfu1(i, j, k);
           f(i, j, k) = (-covc + df);
         }
+    LES_REF_OMP_FOR
     for (int k = 1; k <= km; ++k)
       for (int j = 1; j <= jm; ++j)
         for (int i = 1; i <= im; ++i) {
@@ -527,6 +557,7 @@ struct Ref {
           const T df = vn * dfv1(i, j, k);
           g(i, j, k) = (-covc + df);
         }
+    LES_REF_OMP_FOR
     for (int k = 1; k <= km - 1; ++k)
       for (int j = 1; j <= jm; ++j)
         for (int i = 1; i <= im; ++i) {
@@ -544,6 +575,7 @@ struct Ref {
 
   // ---------------------------------------------------------------- feedbf.f95:35-61
   void feedbf() {
+    LES_REF_OMP_FOR
     for (int k = 1; k <= km; ++k)
       for (int j = 1; j <= jm; ++j)
         for (int i = 1; i <= im; ++i) {
@@ -560,6 +592,7 @@ struct Ref {
           fy(i, j, k) = f1y + f2y;
           fz(i, j, k) = f1z + f2z;
         }
+    LES_REF_OMP_FOR
     for (int k = 1; k <= km; ++k)
       for (int j = 1; j <= jm; ++j)
         for (int i = 1; i <= im; ++i) {
@@ -593,8 +626,10 @@ struct Ref {
     FA<T> &diu1 = diu[1], &diu2 = diu[2], &diu3 = diu[3], &diu4 = diu[4], &diu5 = diu[5],
           &diu6 = diu[6], &diu7 = diu[7], &diu8 = diu[8], &diu9 = diu[9];
     const T cs0 = L(.1);
+    LES_REF_OMP_FOR
     for (int k = 1; k <= km; ++k)
       delx1(k) = std::pow(dx1(0) * dy1(0) * dzn(k), L(1.) / L(3.));   // les.f95:38-42
+    LES_REF_OMP_FOR
     for (int k = 1; k <= km; ++k)
       for (int j = 1; j <= jm; ++j)
         for (int i = 1; i <= im; ++i) {
@@ -616,6 +651,7 @@ struct Ref {
         }
     boundsm();
     // x-component (les.f95:83-114)
+    LES_REF_OMP_FOR
     for (int k = 2; k <= km; ++k)
       for (int j = 1; j <= jm; ++j)
         for (int i = 1; i <= im; ++i) {
@@ -668,6 +704,7 @@ struct Ref {
         f(i, j, 1) = (f(i, j, 1) + vfu);
       }
     // y-component (les.f95:143-174)
+    LES_REF_OMP_FOR
     for (int k = 2; k <= km; ++k)
       for (int j = 1; j <= jm; ++j)
         for (int i = 1; i <= im; ++i) {
@@ -719,6 +756,7 @@ struct Ref {
         g(i, j, 1) = (g(i, j, 1) + vfv);
       }
     // z-component (les.f95:206-242)
+    LES_REF_OMP_FOR
     for (int k = 1; k <= km; ++k)
       for (int j = 1; j <= jm; ++j)
         for (int i = 1; i <= im; ++i) {
@@ -749,6 +787,7 @@ struct Ref {
 
   // ---------------------------------------------------------------- adam.f95:30-44
   void adam() {
+    LES_REF_OMP_FOR
     for (int k = 1; k <= km; ++k)
       for (int j = 1; j <= jm; ++j)
         for (int i = 1; i <= im; ++i) {
@@ -801,6 +840,7 @@ struct Ref {
   // the same FP32 terms; the mean is then rounded back to FP32.
   void press() {
     bondfg();
+    LES_REF_OMP_FOR
     for (int k = 1; k <= km; ++k)
       for (int j = 1; j <= jm; ++j)
         for (int i = 1; i <= im; ++i) {
@@ -825,6 +865,7 @@ struct Ref {
       else { rhsav = s / a; last_area = (double)a; }
     }
     last_rhsav = (double)rhsav;
+    LES_REF_OMP_FOR
     for (int k = 1; k <= km; ++k)
       for (int j = 1; j <= jm; ++j)
         for (int i = 1; i <= im; ++i) rhs(i, j, k) = rhs(i, j, k) - rhsav;
@@ -835,6 +876,32 @@ struct Ref {
       T sor = L(0.0);
       double sord = 0.0;
       for (int nrd = 0; nrd <= 1; ++nrd) {
+#if defined(_OPENMP) && defined(LES_REF_PAR)
+        std::vector<T> sk(km + 1, L(0.0));
+        std::vector<double> sdk(km + 1, 0.0);
+        LES_REF_OMP_FOR
+        for (int k = 1; k <= km; ++k) {
+          T s1 = L(0.0);
+          double sd1 = 0.0;
+          for (int j = 1; j <= jm; ++j)
+            for (int i = 1 + (k + j + nrd) % 2; i <= im; i += 2) {
+              const T reltmp = omega * (cn1(i, j, k) * (cn2l(i) * p(i + 1, j, k) + cn2s(i) * p(i - 1, j, k) +
+                                                        cn3l(j) * p(i, j + 1, k) + cn3s(j) * p(i, j - 1, k) +
+                                                        cn4l(k) * p(i, j, k + 1) + cn4s(k) * p(i, j, k - 1) -
+                                                        rhs(i, j, k)) -
+                                        p(i, j, k));
+              p(i, j, k) = p(i, j, k) + reltmp;
+              if (red64) sd1 += (double)(reltmp * reltmp);
+              else s1 = s1 + reltmp * reltmp;
+            }
+          sk[k] = s1;
+          sdk[k] = sd1;
+        }
+        for (int k = 1; k <= km; ++k) {
+          sor = sor + sk[k];
+          sord += sdk[k];
+        }
+#else
         for (int k = 1; k <= km; ++k)
           for (int j = 1; j <= jm; ++j)
             for (int i = 1 + (k + j + nrd) % 2; i <= im; i += 2) {
@@ -847,6 +914,7 @@ struct Ref {
               if (red64) sord += (double)(reltmp * reltmp);
               else sor = sor + reltmp * reltmp;
             }
+#endif
         boundp1();
       }
       boundp2();
@@ -872,6 +940,7 @@ struct Ref {
       else { pav = s / c; last_pco = (double)c; }
     }
     last_pav = (double)pav;
+    LES_REF_OMP_FOR
     for (int k = 1; k <= km; ++k)
       for (int j = 1; j <= jm; ++j)
         for (int i = 1; i <= im; ++i) p(i, j, k) = p(i, j, k) - pav;
