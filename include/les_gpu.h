@@ -80,7 +80,20 @@ enum les_field {
   /* 2-D inflow planes applied by bondv1 on i = 0, 1 (replace bondv1.f95:33-54) */
   LES_FIELD_UIN = 53,   /* (1:jm, 1:km) */
   LES_FIELD_VIN = 54,
-  LES_FIELD_WIN = 55
+  LES_FIELD_WIN = 55,
+  /* time averages of les_gpu_aveflow (aveflow.f95:7-22), download only, available
+   * after its first call */
+  LES_FIELD_AVEU = 100,    /* (1:im, 1:jm, 0:km)   */
+  LES_FIELD_AVEV = 101,    /* (1:im, 1:jm, 0:km)   */
+  LES_FIELD_AVEW = 102,    /* (1:im+1, 1:jm, 0:km+2) */
+  LES_FIELD_AVEP = 103,    /* (1:im, 1:jm, 1:km) for this one and the rest */
+  LES_FIELD_AVEL = 104,
+  LES_FIELD_AVEUU = 105,
+  LES_FIELD_AVEVV = 106,
+  LES_FIELD_AVEWW = 107,
+  LES_FIELD_AVESM = 108,
+  LES_FIELD_AVESMSM = 109,
+  LES_FIELD_UWFX = 110
 };
 
 typedef struct les_dims {
@@ -234,6 +247,14 @@ int les_batch_sync(les_batch *b);
 /* *n = the member's next step index (> nmax once finished). */
 int les_batch_slot(les_batch *b, int slot, int *n, int *nmax);
 int les_batch_last_error(les_batch *b, char *buf, size_t len);
+
+/* aveflow(n,n1,...,nmax) of aveflow.f95:5-200, called after each step as main.f95:320
+ * does: from step n1 on the time averages (LES_FIELD_AVEU..UWFX) accumulate v, p, u, w,
+ * the squares of u, v, w, sm, sm and the u-w flux; at n == nmax they are divided by
+ * nmax-n1+1 and the rms fluctuations and the mean-removed flux formed.  The averaging
+ * arrays (11 fields) are allocated on the first call.  The reference's unformatted
+ * writes of the averages (data10, data11) are the host's: download the fields. */
+int les_gpu_aveflow(les_handle *h, int n, int n1, int nmax);
 
 /* Tile shape of press's fused SOR sweep.  nx: float4 columns per tile row, 32 (120
  * interior i cells) or 16 (56 cells, uniform cn1 only); ny: tile rows, 16/20/24/28

@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "../../include/les_gpu.h"
+#include "les_aveflow.cuh"
 #include "les_common.cuh"
 #include "les_kernels.cuh"
 #include "les_step.cuh"
@@ -56,12 +57,18 @@ bool declared_extents(int id, int im, int jm, int km, Ext *e) {
     case LES_FIELD_CN3L: case LES_FIELD_CN3S: set(1, jm, 0, 0, 0, 0); return true;
     case LES_FIELD_CN4L: case LES_FIELD_CN4S: case LES_FIELD_DELX1: set(1, km, 0, 0, 0, 0); return true;
     case LES_FIELD_UIN: case LES_FIELD_VIN: case LES_FIELD_WIN: set(1, jm, 1, km, 0, 0); return true;
+    case LES_FIELD_AVEU: case LES_FIELD_AVEV: set(1, im, 1, jm, 0, km); return true;
+    case LES_FIELD_AVEW: set(1, im + 1, 1, jm, 0, km + 2); return true;
+    case LES_FIELD_AVEP: case LES_FIELD_AVEL: case LES_FIELD_AVEUU: case LES_FIELD_AVEVV: case LES_FIELD_AVEWW:
+    case LES_FIELD_AVESM: case LES_FIELD_AVESMSM: case LES_FIELD_UWFX: set(1, im, 1, jm, 1, km); return true;
     default: return false;
   }
 }
 
 bool is_1d(int id) { return id >= LES_FIELD_DX1 && id <= LES_FIELD_DELX1; }
 bool is_inflow(int id) { return id >= LES_FIELD_UIN && id <= LES_FIELD_WIN; }
+bool is_ave(int id) { return id >= LES_FIELD_AVEU && id <= LES_FIELD_UWFX; }
+constexpr int kNumAve = LES_FIELD_UWFX - LES_FIELD_AVEU + 1;
 
 }  // namespace
 
@@ -112,6 +119,7 @@ struct les_handle {
     long long ticket = -1;
   };
   static constexpr int kDlSlots = 8;
+  float *ave_d[kNumAve] = {};  // aveflow's averaging arrays (les_gpu_aveflow allocates them)
   DlSlot dl[kDlSlots];
   cudaStream_t cs = nullptr;
   long long next_ticket = 0;
@@ -265,6 +273,7 @@ extern "C" int les_gpu_destroy(les_handle *h) {
     if (sl.done) cudaEventDestroy(sl.done);
   }
   if (h->cs) cudaStreamDestroy(h->cs);
+  for (float *a : h->ave_d) cudaFree(a);
   les_step_plan_free(&h->plan);
   for (int f = 0; f < kNumFields; ++f) cudaFree(h->fields[f]);
   cudaFree(h->mask_d);
@@ -409,7 +418,8 @@ int download_async(les_handle *h, int field, float *host, const int lb[3], const
   }
   const unsigned rows = (unsigned)ny * (unsigned)nz;
   if (rows > 0) {
-    k_pack_box<<<rows, 128, 0, h->s>>>(h->fields[field - 1], sl.buf, h->pi, h->nj, lb[0], lb[1], lb[2], nx, ny);
+    const float *src = is_ave(field) ? h->ave_d[field - LES_FIELD_AVEU] : h->fields[field - 1];
+    k_pack_box<<<rows, 128, 0, h->s>>>(src, sl.buf, h->pi, h->nj, lb[0], lb[1], lb[2], nx, ny);
     CK(h, cudaGetLastError());
   }
   CK(h, cudaEventRecord(sl.packed, h->s));
@@ -437,7 +447,11 @@ extern "C" int les_gpu_download_async(les_handle *h, int field, float *host, con
   Ext decl;
   int rc = check_ext(h, field, lb, ub, &decl);
   if (rc) return rc;
-  if (field < LES_FIELD_U || field > LES_FIELD_SM) return fail(h, LES_ERR_ARG, "download_async: 3-D fields only");
+  if (is_ave(field)) {
+    if (!h->ave_d[0]) return fail(h, LES_ERR_STATE, "download_async: les_gpu_aveflow not called yet");
+  } else if (field < LES_FIELD_U || field > LES_FIELD_SM) {
+    return fail(h, LES_ERR_ARG, "download_async: 3-D fields only");
+  }
   return download_async(h, field, host, lb, ub, ticket);
 }
 
@@ -451,7 +465,8 @@ extern "C" int les_gpu_download(les_handle *h, int field, float *host, const int
   Ext decl;
   int rc = check_ext(h, field, lb, ub, &decl);
   if (rc) return rc;
-  if (field >= LES_FIELD_U && field <= LES_FIELD_SM) {
+  if ((field >= LES_FIELD_U && field <= LES_FIELD_SM) || is_ave(field)) {
+    if (is_ave(field) && !h->ave_d[0]) return fail(h, LES_ERR_STATE, "download: les_gpu_aveflow not called yet");
     long long t = -1;
     rc = download_async(h, field, host, lb, ub, &t);
     if (rc) return rc;
@@ -815,6 +830,25 @@ extern "C" int les_gpu_diag(les_handle *h, double out[5]) {
   out[3] = sc[SC_RHSAV];
   out[4] = sc[SC_PAV];
   return LES_OK;
+}
+
+extern "C" int les_gpu_aveflow(les_handle *h, int n, int n1, int nmax) {
+  NEED_COMMIT(h);
+  if (n1 < 1 || nmax < n1) return fail(h, LES_ERR_ARG, "aveflow: need 1 <= n1 <= nmax");
+  if (!h->ave_d[0]) {
+    for (int q = 0; q < kNumAve; ++q) {
+      if (cudaMalloc(&h->ave_d[q], h->nfloat * sizeof(float)) != cudaSuccess) {
+        (void)cudaGetLastError();
+        for (float *&a : h->ave_d) { cudaFree(a); a = nullptr; }
+        return fail(h, LES_ERR_NOMEM, "aveflow: no device memory for the averaging arrays");
+      }
+      CK(h, cudaMemsetAsync(h->ave_d[q], 0, h->nfloat * sizeof(float), h->s));
+    }
+  }
+  float **a = h->ave_d;
+  const LesAve A{a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7], a[8], a[9], a[10]};
+  les_launch_aveflow(h->dom, A, n, n1, nmax, ctx_of(h));
+  return check_launch(h, "aveflow");
 }
 
 extern "C" int les_gpu_set_sor_shape(les_handle *h, int nx, int ny, int kchunk) {

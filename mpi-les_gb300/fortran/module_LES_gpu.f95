@@ -95,6 +95,11 @@ module module_LES_gpu
       type(c_ptr), value :: h
       integer(c_long_long), value :: ticket
     end function
+    integer(c_int) function les_gpu_aveflow(h, n, n1, nmax) bind(C, name='les_gpu_aveflow')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h
+      integer(c_int), value :: n, n1, nmax
+    end function
     integer(c_int) function les_gpu_commit_setup(h) bind(C, name='les_gpu_commit_setup')
       import :: c_int, c_ptr
       type(c_ptr), value :: h

@@ -26,10 +26,15 @@ U, V, W, P, F, G, H, FOLD, GOLD, HOLD, USUM, VSUM, WSUM, RHS, SM = range(1, 16)
 BMASK1, CMASK1, DMASK1, CN1 = 16, 17, 18, 20
 DX1, DY1, DZN, DZS, DXS, DYS, Z2, CN2L, CN2S, CN3L, CN3S, CN4L, CN4S, DELX1 = range(32, 46)
 UIN, VIN, WIN = 53, 54, 55
+# time averages of Domain.aveflow (aveflow.f95:7-22), download only
+AVEU, AVEV, AVEW, AVEP, AVEL, AVEUU, AVEVV, AVEWW, AVESM, AVESMSM, UWFX = range(100, 111)
+AVE_FIELDS = (AVEU, AVEV, AVEW, AVEP, AVEL, AVEUU, AVEVV, AVEWW, AVESM, AVESMSM, UWFX)
 
 FIELD_NAMES = {
     U: "u", V: "v", W: "w", P: "p", F: "f", G: "g", H: "h", FOLD: "fold", GOLD: "gold",
     HOLD: "hold", USUM: "usum", VSUM: "vsum", WSUM: "wsum", RHS: "rhs", SM: "sm",
+    AVEU: "aveu", AVEV: "avev", AVEW: "avew", AVEP: "avep", AVEL: "avel", AVEUU: "aveuu", AVEVV: "avevv",
+    AVEWW: "aveww", AVESM: "avesm", AVESMSM: "avesmsm", UWFX: "uwfx",
 }
 STATE_FIELDS = (U, V, W, P, F, G, H, FOLD, GOLD, HOLD, USUM, VSUM, WSUM)
 
@@ -61,6 +66,12 @@ def declared_extents(fid: int, im: int, jm: int, km: int):
         return (lo, 0, 0), (hi, 0, 0)
     if fid in (UIN, VIN, WIN):
         return (1, 1, 0), (jm, km, 0)
+    if fid in (AVEU, AVEV):
+        return (1, 1, 0), (im, jm, km)
+    if fid == AVEW:
+        return (1, 1, 0), (im + 1, jm, km + 2)
+    if fid in AVE_FIELDS:
+        return (1, 1, 1), (im, jm, km)
     raise KeyError(fid)
 
 
@@ -183,6 +194,7 @@ def load_library(path: str | None = None) -> C.CDLL:
         "les_gpu_last_error": (C.c_int, [vp, C.c_char_p, C.c_size_t]),
         "les_gpu_profile": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(C.c_double)]),
         "les_gpu_set_sor_shape": (C.c_int, [vp, C.c_int, C.c_int, C.c_int]),
+        "les_gpu_aveflow": (C.c_int, [vp, C.c_int, C.c_int, C.c_int]),
         "les_gpu_sor_shape": (C.c_int, [vp, C.POINTER(C.c_int)]),
         "les_gpu_tune_sor": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double), C.c_char_p,
                                        C.c_size_t]),
@@ -413,6 +425,11 @@ class Domain:
         s = C.c_void_p()
         self._check(self.lib.les_gpu_stream(self._h, C.byref(s)), "stream")
         return s.value or 0
+
+    def aveflow(self, n: int, n1: int, nmax: int) -> None:
+        """aveflow.f95 after step n: time averages from step n1, finalised at nmax
+        (download AVEU..UWFX)."""
+        self._check(self.lib.les_gpu_aveflow(self._h, n, n1, nmax), "aveflow")
 
     def set_sor_shape(self, nx: int = 0, ny: int = 0, kchunk: int = 0) -> None:
         """Fix the SOR sweep's tile shape (0 = automatic); see les_gpu_set_sor_shape."""

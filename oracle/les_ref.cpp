@@ -104,6 +104,9 @@ struct Ref {
   FA<T> uspd, vspd, zbm, uin, vin, win;
   FA<T> nou[10], diu[10], cov[10];
   FA<T> dfu1, dfv1, dfw1;
+  // aveflow.f95:7-22 (time averages; allocated on the first aveflow call)
+  FA<T> aveu, avev, avew, avep, avel, aveuu, avevv, aveww, avesm, avesmsm, uwfx;
+  bool ave_alloc = false;
 
   // diagnostics of the last step
   int last_iters = 0;
@@ -959,6 +962,88 @@ struct Ref {
     press();
   }
 
+  // ---------------------------------------------------------------- aveflow.f95:5-200
+  // Time averages of v, p, u, w, of the squares of u, v, w, sm, of sm and of the u-w
+  // flux from step n1 on, finalised at n == nmax (the unformatted writes of
+  // :200-350 are the host's: the arrays are read back instead).  x**2 is x*x.
+  void aveflow(int n, int n1, int nmax) {
+    if (!ave_alloc) {
+      const int ip = im, jp = jm, kp = km;
+      aveu.alloc("aveu", 1, ip, 1, jp, 0, kp); avev.alloc("avev", 1, ip, 1, jp, 0, kp);
+      avew.alloc("avew", 1, ip + 1, 1, jp, 0, kp + 2);
+      avep.alloc("avep", 1, ip, 1, jp, 1, kp); avel.alloc("avel", 1, ip, 1, jp, 1, kp);
+      aveuu.alloc("aveuu", 1, ip, 1, jp, 1, kp); avevv.alloc("avevv", 1, ip, 1, jp, 1, kp);
+      aveww.alloc("aveww", 1, ip, 1, jp, 1, kp); avesm.alloc("avesm", 1, ip, 1, jp, 1, kp);
+      avesmsm.alloc("avesmsm", 1, ip, 1, jp, 1, kp); uwfx.alloc("uwfx", 1, ip, 1, jp, 1, kp);
+      ave_alloc = true;
+    }
+    if (n == n1) {  // :82-114
+      for (int k = 1; k <= km; ++k)
+        for (int j = 1; j <= jm; ++j)
+          for (int i = 1; i <= im; ++i) {
+            avev(i, j, k) = L(0.0); avep(i, j, k) = L(0.0); avel(i, j, k) = L(0.0);
+            aveuu(i, j, k) = L(0.0); avevv(i, j, k) = L(0.0); aveww(i, j, k) = L(0.0);
+            avesm(i, j, k) = L(0.0); avesmsm(i, j, k) = L(0.0); uwfx(i, j, k) = L(0.0);
+          }
+      for (int k = 0; k <= km; ++k)
+        for (int j = 1; j <= jm; ++j)
+          for (int i = 1; i <= im; ++i) aveu(i, j, k) = L(0.0);
+      for (int k = 0; k <= km; ++k)
+        for (int j = 1; j <= jm; ++j)
+          for (int i = 1; i <= im + 1; ++i) avew(i, j, k) = L(0.0);
+    }
+    if (n >= n1) {  // :117-149
+      for (int k = 1; k <= km; ++k)
+        for (int j = 1; j <= jm; ++j)
+          for (int i = 1; i <= im; ++i) {
+            avev(i, j, k) = avev(i, j, k) + v(i, j, k);
+            avep(i, j, k) = avep(i, j, k) + p(i, j, k);
+            aveuu(i, j, k) = aveuu(i, j, k) + u(i, j, k) * u(i, j, k);
+            avevv(i, j, k) = avevv(i, j, k) + v(i, j, k) * v(i, j, k);
+            aveww(i, j, k) = aveww(i, j, k) + w(i, j, k) * w(i, j, k);
+            avesm(i, j, k) = avesm(i, j, k) + sm(i, j, k);
+            avesmsm(i, j, k) = avesmsm(i, j, k) + sm(i, j, k) * sm(i, j, k);
+            uwfx(i, j, k) = uwfx(i, j, k) + L(0.5) * (u(i, j, k - 1) + u(i, j, k)) * L(0.5) *
+                                                (w(i, j, k - 1) + w(i + 1, j, k - 1));
+          }
+      for (int k = 0; k <= km; ++k)
+        for (int j = 1; j <= jm; ++j)
+          for (int i = 1; i <= im; ++i) aveu(i, j, k) = aveu(i, j, k) + u(i, j, k);
+      for (int k = 0; k <= km; ++k)
+        for (int j = 1; j <= jm; ++j)
+          for (int i = 1; i <= im + 1; ++i) avew(i, j, k) = avew(i, j, k) + w(i, j, k);
+    }
+    if (n == nmax) {  // :151-200
+      const T cnt = (T)(nmax - n1 + 1);  // float(nmax-n1+1)
+      for (int k = 1; k <= km; ++k)
+        for (int j = 1; j <= jm; ++j)
+          for (int i = 1; i <= im; ++i) {
+            avev(i, j, k) = avev(i, j, k) / cnt; avep(i, j, k) = avep(i, j, k) / cnt;
+            avel(i, j, k) = avel(i, j, k) / cnt; aveuu(i, j, k) = aveuu(i, j, k) / cnt;
+            avevv(i, j, k) = avevv(i, j, k) / cnt; aveww(i, j, k) = aveww(i, j, k) / cnt;
+            avesm(i, j, k) = avesm(i, j, k) / cnt; avesmsm(i, j, k) = avesmsm(i, j, k) / cnt;
+          }
+      for (int k = 0; k <= km; ++k)
+        for (int j = 1; j <= jm; ++j)
+          for (int i = 1; i <= im; ++i) aveu(i, j, k) = aveu(i, j, k) / cnt;
+      for (int k = 0; k <= km; ++k)
+        for (int j = 1; j <= jm; ++j)
+          for (int i = 1; i <= im + 1; ++i) avew(i, j, k) = avew(i, j, k) / cnt;
+      for (int k = 1; k <= km; ++k)
+        for (int j = 1; j <= jm; ++j)
+          for (int i = 1; i <= im; ++i)
+            uwfx(i, j, k) = uwfx(i, j, k) / cnt - L(0.5) * (aveu(i, j, k - 1) + aveu(i, j, k)) * L(0.5) *
+                                                      (avew(i, j, k - 1) + avew(i + 1, j, k - 1));
+      for (int k = 1; k <= km; ++k)
+        for (int j = 1; j <= jm; ++j)
+          for (int i = 1; i <= im; ++i) {
+            aveuu(i, j, k) = std::sqrt(std::abs(aveuu(i, j, k) - aveu(i, j, k) * aveu(i, j, k)));
+            avevv(i, j, k) = std::sqrt(std::abs(avevv(i, j, k) - avev(i, j, k) * avev(i, j, k)));
+            aveww(i, j, k) = std::sqrt(std::abs(aveww(i, j, k) - avew(i, j, k) * avew(i, j, k)));
+          }
+    }
+  }
+
   FA<T> *field(int id) {
     switch (id) {
       case 1: return &u; case 2: return &v; case 3: return &w; case 4: return &p;
@@ -977,6 +1062,14 @@ struct Ref {
       case 90: return &fx; case 91: return &fy; case 92: return &fz;
       case 93: return &dfu1; case 94: return &dfv1; case 95: return &dfw1;
       default: break;
+    }
+    if (ave_alloc) {  // aveflow arrays (product ids LES_FIELD_AVEU..LES_FIELD_UWFX)
+      switch (id) {
+        case 100: return &aveu; case 101: return &avev; case 102: return &avew; case 103: return &avep;
+        case 104: return &avel; case 105: return &aveuu; case 106: return &avevv; case 107: return &aveww;
+        case 108: return &avesm; case 109: return &avesmsm; case 110: return &uwfx;
+        default: break;
+      }
     }
     if (id >= 60 && id <= 68) return &diu[id - 59];
     if (id >= 70 && id <= 78) return &cov[id - 69];
@@ -1090,6 +1183,20 @@ int ref_stage(void *hv, int s, int n, int nmax) {
   Handle *h = (Handle *)hv;
   try {
     return h->f64 ? stage(h->f64, s, n, nmax) : stage(h->f32, s, n, nmax);
+  } catch (const RefError &e) {
+    g_err = e.msg;
+  } catch (const std::exception &e) {
+    g_err = e.what();
+  }
+  return -3;
+}
+
+int ref_aveflow(void *hv, int n, int n1, int nmax) {
+  Handle *h = (Handle *)hv;
+  try {
+    if (h->f64) h->f64->aveflow(n, n1, nmax);
+    else h->f32->aveflow(n, n1, nmax);
+    return 0;
   } catch (const RefError &e) {
     g_err = e.msg;
   } catch (const std::exception &e) {

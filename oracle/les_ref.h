@@ -54,6 +54,9 @@ void *ref_create(int prec, int im, int jm, int km, const double *consts, const i
                  const float *zbm, const float *uin, const float *vin, const float *win);
 void ref_destroy(void *h);
 int ref_stage(void *h, int stage, int n, int nmax);
+/* aveflow.f95:5-200 at step n with averaging from step n1 to nmax (the time averages,
+ * fields 100..110, exist after the first call) */
+int ref_aveflow(void *h, int n, int n1, int nmax);
 /* copy a field (Fortran extents lb..ub, i fastest) out of / into the oracle */
 int ref_get(void *h, int field, double *out, const int *lb, const int *ub);
 int ref_set(void *h, int field, const double *in, const int *lb, const int *ub);

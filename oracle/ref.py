@@ -45,6 +45,8 @@ def load(fast: bool = False) -> C.CDLL:
     lib.ref_destroy.argtypes = [vp]
     lib.ref_stage.restype = C.c_int
     lib.ref_stage.argtypes = [vp, C.c_int, C.c_int, C.c_int]
+    lib.ref_aveflow.restype = C.c_int
+    lib.ref_aveflow.argtypes = [vp, C.c_int, C.c_int, C.c_int]
     for n in ("ref_get", "ref_set"):
         getattr(lib, n).restype = C.c_int
         getattr(lib, n).argtypes = [vp, C.c_int, dp, ip_, ip_]
@@ -93,6 +95,11 @@ class Ref:
 
     def step(self, n: int, nmax: int):
         self.stage(STEP, n, nmax)
+
+    def aveflow(self, n: int, n1: int, nmax: int):
+        """aveflow.f95: accumulate the time averages at step n (from n1), finalise at nmax."""
+        if self.lib.ref_aveflow(self._h, n, n1, nmax):
+            raise RuntimeError("ref_aveflow: " + self.lib.ref_last_error().decode())
 
     def extents(self, fid: int):
         lb, ub = (C.c_int * 3)(), (C.c_int * 3)()

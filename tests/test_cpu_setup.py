@@ -35,6 +35,7 @@ def test_library_exports_every_declared_symbol(built_lib):
 def test_field_ids_match_oracle(built_lib):
     sc = scenario(12, 8, 6)
     r = make_ref(4, sc)
+    r.aveflow(1, 1, 1)  # the time-average fields exist from the first aveflow on
     for fid in list(lesgpu.FIELD_NAMES) + [lesgpu.BMASK1, lesgpu.CMASK1, lesgpu.DMASK1, lesgpu.CN1]:
         lb, ub = lesgpu.declared_extents(fid, sc.im, sc.jm, sc.km)
         assert r.extents(fid) == (lb, ub), fid
