@@ -40,6 +40,7 @@ extern "C" {
 #define LES_ERR_NOMEM (-4)    /* device memory exhausted                            */
 #define LES_ERR_NUMERIC (-5)  /* non-finite values detected by les_gpu_check_finite */
 #define LES_ERR_BUSY (-6)     /* batch slot or request refused (capacity)           */
+#define LES_ERR_IO (-7)       /* a file could not be opened, written or read        */
 
 /* Field ids.  3-D state and work arrays (extents as declared in src/main.f95:63-159). */
 enum les_field {
@@ -255,6 +256,38 @@ int les_batch_last_error(les_batch *b, char *buf, size_t len);
  * arrays (11 fields) are allocated on the first call.  The reference's unformatted
  * writes of the averages (data10, data11) are the host's: download the fields. */
 int les_gpu_aveflow(les_handle *h, int n, int n1, int nmax);
+
+/* ---- the reference's result and restart files ----------------------------------
+ * gfortran unformatted sequential files, one record per Fortran write, each 3-D record
+ * the interior box (1:im,1:jm,1:km), i fastest.  Big-endian markers and values, as the
+ * reference is built (SConstruct:77, -fconvert=big-endian), unless flags has
+ * LES_IO_LITTLE_ENDIAN.  Records over 2147483639 bytes are split into gfortran
+ * subrecords (LES_IO_MAX_SUBRECORD in the environment lowers that limit, like
+ * -fmax-subrecord-length).  The writers download the fields (they synchronise the
+ * handle's stream); the reader uploads them.  The reference writes data20 and data21
+ * when mod(n,1000) == 0 or n == nmax (press.f95:197, adam.f95:21): the caller keeps
+ * that test around les_gpu_write_data20/21. */
+#define LES_IO_LITTLE_ENDIAN 1
+/* press.f95:205-216: u, v, w, p, usum, vsum, wsum */
+int les_gpu_write_data20(les_handle *h, const char *path, int flags);
+/* adam.f95:20-27: fold, gold, hold, fghold (never assigned in the reference: zeros) */
+int les_gpu_write_data21(les_handle *h, const char *path, int flags);
+/* anime.f95:370-490: the record (n, time) as int32 and real(4), then u, v, w, p, usum,
+ * vsum, wsum */
+int les_gpu_write_data30(les_handle *h, const char *path, int n, float time, int flags);
+/* anime.f95:492-595: f, g, h, fold, gold, hold */
+int les_gpu_write_data31(les_handle *h, const char *path, int flags);
+/* ifdata_out(n,n0,n1,nmax,time,...) of anime.f95:326, called after every step
+ * (main.f95:318): when n == n1-1 or n == nmax it writes <dir>/data30NNNNNN.dat and
+ * <dir>/data31NNNNNN.dat (NNNNNN = n as i6.6) and sets *written (may be NULL) to 1;
+ * otherwise it writes nothing and sets it to 0. */
+int les_gpu_ifdata_out(les_handle *h, const char *dir, int n, int n1, int nmax, float time, int flags,
+                       int *written);
+/* The restart read of ifdata (ifdata.f95:252-480, ical == 1): n and time from data30's
+ * first record, then the interiors (1:im,1:jm,1:km) of u, v, w, p, usum, vsum, wsum from
+ * data30 and of f, g, h, fold, gold, hold from data31; halos keep their values.  Either
+ * byte order is read.  A record shorter than im*jm*km values fails with LES_ERR_IO. */
+int les_gpu_read_restart(les_handle *h, const char *data30, const char *data31, int *n, float *time);
 
 /* Tile shape of press's fused SOR sweep.  nx: float4 columns per tile row, 32 (120
  * interior i cells) or 16 (56 cells, uniform cn1 only); ny: tile rows, 16/20/24/28

@@ -993,3 +993,15 @@ extern "C" int les_gpu_profile(les_handle *h, int what, int reps, double *ms_avg
   *ms_avg = (double)ms / reps / per_rep;
   return check_launch(h, "profile");
 }
+
+// Handle access for the file readers and writers of les_io.cpp (host code that sits on
+// the entry points above).
+int les_handle_dims(const les_handle *h, int *im, int *jm, int *km) {
+  if (!h) return LES_ERR_ARG;
+  *im = h->dims.im;
+  *jm = h->dims.jm;
+  *km = h->dims.km;
+  return LES_OK;
+}
+
+int les_handle_fail(les_handle *h, int code, const char *msg) { return fail(h, code, msg); }

@@ -32,6 +32,7 @@ module module_LES_gpu
   private
   public :: initialise_LES_gpu, run_LES_gpu, sync_LES_gpu, finalise_LES_gpu
   public :: velnw, bondv1, velfg, feedbf, les, adam, press, boundp1, boundp2
+  public :: ifdata_out, read_restart_LES_gpu
 
   ! field ids of include/les_gpu.h
   integer(c_int), parameter :: LES_FIELD_U = 1, LES_FIELD_V = 2, LES_FIELD_W = 3, LES_FIELD_P = 4
@@ -99,6 +100,34 @@ module module_LES_gpu
       import :: c_int, c_ptr
       type(c_ptr), value :: h
       integer(c_int), value :: n, n1, nmax
+    end function
+    integer(c_int) function les_gpu_write_data20(h, path, flags) bind(C, name='les_gpu_write_data20')
+      import :: c_int, c_ptr, c_char
+      type(c_ptr), value :: h
+      character(kind=c_char), dimension(*) :: path
+      integer(c_int), value :: flags
+    end function
+    integer(c_int) function les_gpu_write_data21(h, path, flags) bind(C, name='les_gpu_write_data21')
+      import :: c_int, c_ptr, c_char
+      type(c_ptr), value :: h
+      character(kind=c_char), dimension(*) :: path
+      integer(c_int), value :: flags
+    end function
+    integer(c_int) function les_gpu_ifdata_out(h, dir, n, n1, nmax, time, flags, written) &
+        bind(C, name='les_gpu_ifdata_out')
+      import :: c_int, c_ptr, c_char, c_float
+      type(c_ptr), value :: h
+      character(kind=c_char), dimension(*) :: dir
+      integer(c_int), value :: n, n1, nmax, flags
+      real(c_float), value :: time
+      integer(c_int) :: written
+    end function
+    integer(c_int) function les_gpu_read_restart(h, data30, data31, n, time) bind(C, name='les_gpu_read_restart')
+      import :: c_int, c_ptr, c_char, c_float
+      type(c_ptr), value :: h
+      character(kind=c_char), dimension(*) :: data30, data31
+      integer(c_int) :: n
+      real(c_float) :: time
     end function
     integer(c_int) function les_gpu_commit_setup(h) bind(C, name='les_gpu_commit_setup')
       import :: c_int, c_ptr
@@ -346,13 +375,18 @@ contains
     call check(les_gpu_les(les_h), 'les')
   end subroutine
 
-  ! The reference's adam also writes data21 (fold, gold, hold) at n == nmax
-  ! (adam.f95:20-29): call sync_LES_gpu first and write from the host arrays.
+  ! adam writes data21 (fold, gold, hold, fghold) when mod(n,1000) == 0 or n == nmax
+  ! (adam.f95:20-27), from the device state, big-endian like the reference's build.
   subroutine adam(n, nmax, data21, fold, im, jm, km, gold, hold, fghold, f, g, h)
     integer, intent(in) :: n, nmax, im, jm, km
     character(len=*) :: data21
     real(4) :: fold(*), gold(*), hold(*), fghold(*), f(*), g(*), h(*)
     call check(les_gpu_adam(les_h), 'adam')
+#if !defined(NO_IO) && !defined(MPI)
+    if (mod(n, 1000) == 0 .or. n == nmax) then
+      call check(les_gpu_write_data21(les_h, trim(data21)//c_null_char, 0_c_int), 'adam: data21')
+    end if
+#endif
   end subroutine
 
   subroutine press(km, jm, im, rhs, u, dx1, v, dy1, w, dzn, f, g, h, dt, cn1, cn2l, p, cn2s, cn3l, cn3s, &
@@ -363,6 +397,40 @@ contains
     real(4) :: rhs(*), u(*), dx1(*), v(*), dy1(*), w(*), dzn(*), f(*), g(*), h(*), cn1(*), cn2l(*)
     real(4) :: p(*), cn2s(*), cn3l(*), cn3s(*), cn4l(*), cn4s(*), usum(*), vsum(*), wsum(*)
     call check(les_gpu_press(les_h, int(n, c_int), int(nmax, c_int)), 'press')
+    ! press.f95:197-216: data20 (u, v, w, p, usum, vsum, wsum) every 1000 steps and at nmax
+#if !defined(NO_IO) && !defined(MPI)
+    if (mod(n, 1000) == 0 .or. n == nmax) then
+      call check(les_gpu_write_data20(les_h, trim(data20)//c_null_char, 0_c_int), 'press: data20')
+    end if
+#endif
+  end subroutine
+
+  ! ifdata_out of anime.f95:326 (called after every step, main.f95:318): data30NNNNNN.dat
+  ! and data31NNNNNN.dat in the working directory at n == n1-1 and n == nmax.
+  subroutine ifdata_out(n, n0, n1, nmax, time, km, jm, im, u, w, v, p, usum, vsum, wsum, f, g, h, &
+                        fold, gold, hold)
+    integer, intent(in) :: n, n0, n1, nmax, km, jm, im
+    real, intent(in) :: time
+    real(4) :: u(*), w(*), v(*), p(*), usum(*), vsum(*), wsum(*), f(*), g(*), h(*)
+    real(4) :: fold(*), gold(*), hold(*)
+    integer(c_int) :: written
+    call check(les_gpu_ifdata_out(les_h, '.'//c_null_char, int(n, c_int), int(n1, c_int), &
+                                  int(nmax, c_int), real(time, c_float), 0_c_int, written), 'ifdata_out')
+  end subroutine
+
+  ! The restart read of ifdata (ifdata.f95:252-480, ical == 1), into the device state:
+  ! n and time from data30, the interiors of the 13 state fields from data30/data31.
+  ! The reference reads 'data30048000.dat' and 'data31048000.dat'.
+  subroutine read_restart_LES_gpu(data30, data31, n, time)
+    character(len=*), intent(in) :: data30, data31
+    integer, intent(out) :: n
+    real, intent(out) :: time
+    integer(c_int) :: nc
+    real(c_float) :: tc
+    call check(les_gpu_read_restart(les_h, trim(data30)//c_null_char, trim(data31)//c_null_char, nc, tc), &
+               'read_restart')
+    n = nc
+    time = tc
   end subroutine
 
   subroutine boundp1(km, jm, p, im)

@@ -41,7 +41,8 @@ STATE_FIELDS = (U, V, W, P, F, G, H, FOLD, GOLD, HOLD, USUM, VSUM, WSUM)
 PROF_SOR, PROF_VELFG, PROF_LES, PROF_VELNW, PROF_STEP = range(5)
 
 ERRORS = {0: "ok", -1: "bad argument", -2: "CUDA error", -3: "call out of order",
-          -4: "out of device memory", -5: "non-finite values", -6: "busy"}
+          -4: "out of device memory", -5: "non-finite values", -6: "busy", -7: "file error"}
+IO_LITTLE_ENDIAN = 1
 
 
 def declared_extents(fid: int, im: int, jm: int, km: int):
@@ -200,6 +201,12 @@ def load_library(path: str | None = None) -> C.CDLL:
                                        C.c_size_t]),
         "les_sor_tuned": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int)]),
         "les_sor_set_tuned": (C.c_int, [C.c_int] * 8),
+        "les_gpu_write_data20": (C.c_int, [vp, C.c_char_p, C.c_int]),
+        "les_gpu_write_data21": (C.c_int, [vp, C.c_char_p, C.c_int]),
+        "les_gpu_write_data30": (C.c_int, [vp, C.c_char_p, C.c_int, C.c_float, C.c_int]),
+        "les_gpu_write_data31": (C.c_int, [vp, C.c_char_p, C.c_int]),
+        "les_gpu_ifdata_out": (C.c_int, [vp, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_float, C.c_int, ip_]),
+        "les_gpu_read_restart": (C.c_int, [vp, C.c_char_p, C.c_char_p, ip_, fp_]),
         "les_batch_create": (C.c_int, [C.POINTER(vp)]),
         "les_batch_destroy": (C.c_int, [vp]),
         "les_batch_admit": (C.c_int, [C.POINTER(LesDims), C.c_size_t, ip_]),
@@ -430,6 +437,49 @@ class Domain:
         """aveflow.f95 after step n: time averages from step n1, finalised at nmax
         (download AVEU..UWFX)."""
         self._check(self.lib.les_gpu_aveflow(self._h, n, n1, nmax), "aveflow")
+
+    # ------------------------------------------------- result and restart files
+    @staticmethod
+    def _io_flags(big_endian: bool) -> int:
+        return 0 if big_endian else IO_LITTLE_ENDIAN
+
+    def write_data20(self, path: str, big_endian: bool = True) -> None:
+        """data20 of press.f95:205-216 (u, v, w, p, usum, vsum, wsum)."""
+        self._check(self.lib.les_gpu_write_data20(self._h, os.fsencode(path), self._io_flags(big_endian)),
+                    "write_data20")
+
+    def write_data21(self, path: str, big_endian: bool = True) -> None:
+        """data21 of adam.f95:20-27 (fold, gold, hold, fghold = zeros)."""
+        self._check(self.lib.les_gpu_write_data21(self._h, os.fsencode(path), self._io_flags(big_endian)),
+                    "write_data21")
+
+    def write_data30(self, path: str, n: int, time: float, big_endian: bool = True) -> None:
+        """data30 of anime.f95:370-490: (n, time), u, v, w, p, usum, vsum, wsum."""
+        self._check(self.lib.les_gpu_write_data30(self._h, os.fsencode(path), n, time,
+                                                  self._io_flags(big_endian)), "write_data30")
+
+    def write_data31(self, path: str, big_endian: bool = True) -> None:
+        """data31 of anime.f95:492-595: f, g, h, fold, gold, hold."""
+        self._check(self.lib.les_gpu_write_data31(self._h, os.fsencode(path), self._io_flags(big_endian)),
+                    "write_data31")
+
+    def ifdata_out(self, directory: str, n: int, n1: int, nmax: int, time: float,
+                   big_endian: bool = True) -> bool:
+        """ifdata_out of anime.f95:326 (after every step, main.f95:318): writes
+        data30NNNNNN.dat and data31NNNNNN.dat into `directory` when n == n1-1 or
+        n == nmax; returns whether it wrote."""
+        w = C.c_int(0)
+        self._check(self.lib.les_gpu_ifdata_out(self._h, os.fsencode(directory), n, n1, nmax, time,
+                                                self._io_flags(big_endian), C.byref(w)), "ifdata_out")
+        return bool(w.value)
+
+    def read_restart(self, data30: str, data31: str) -> tuple[int, float]:
+        """The restart read of ifdata.f95:252-480: loads the interiors of the 13 state
+        fields from data30/data31 (either byte order); returns (n, time)."""
+        n, t = C.c_int(0), C.c_float(0.0)
+        self._check(self.lib.les_gpu_read_restart(self._h, os.fsencode(data30), os.fsencode(data31),
+                                                  C.byref(n), C.byref(t)), "read_restart")
+        return n.value, t.value
 
     def set_sor_shape(self, nx: int = 0, ny: int = 0, kchunk: int = 0) -> None:
         """Fix the SOR sweep's tile shape (0 = automatic); see les_gpu_set_sor_shape."""
