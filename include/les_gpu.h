@@ -59,9 +59,9 @@ enum les_field {
   LES_FIELD_WSUM = 13,
   LES_FIELD_RHS = 14,   /* (0:im+1, 0:jm+1, 0:km+1)  main.f95:145 */
   LES_FIELD_SM = 15,    /* (-1:im+1,-1:jm+1, 0:km+1) main.f95:146 */
-  LES_FIELD_BMASK1 = 16,/* (-1:im+1, 0:jm+1, 0:km+1) upload only; values 0 or 1 */
-  LES_FIELD_CMASK1 = 17,/* (0:im+1,-1:jm+1, 0:km+1)  upload only; values 0 or 1 */
-  LES_FIELD_DMASK1 = 18,/* (0:im+1, 0:jm+1, 0:km+1)  upload only; values 0 or 1 */
+  LES_FIELD_BMASK1 = 16,/* (-1:im+1, 0:jm+1, 0:km+1) values 0 or 1 */
+  LES_FIELD_CMASK1 = 17,/* (0:im+1,-1:jm+1, 0:km+1)  values 0 or 1 */
+  LES_FIELD_DMASK1 = 18,/* (0:im+1, 0:jm+1, 0:km+1)  values 0 or 1 */
   LES_FIELD_CN1 = 20,   /* (1:im, 1:jm, 1:km)        upload only (init.f95:98-104) */
   /* 1-D grid and Poisson coefficient arrays (grid.f95, init.f95:82-95) */
   LES_FIELD_DX1 = 32,   /* (-1:im+1) */
@@ -148,6 +148,13 @@ int les_setup_poisson(int im, int jm, int km, const float *dxs, const float *dys
 int les_setup_masks(int im, int jm, int km, const float *zbm, const float *z2,
                     const float *dzn, float *amask1, float *bmask1, float *cmask1,
                     float *dmask1);
+/* The interior volume sum(dx1(i)*dy1(j)*dzn(k)) that rhsav and pav divide by
+ * (press.f95:65-72, 124-133): each product rounded to FP32, summed in FP64 in the
+ * loop order k, j, i.  dx1(-1:im+1), dy1(0:jm+1), dzn(-1:km+2).  O(im + jm + km x
+ * distinct (dx1, dy1) pairs) when the partial sums are provably exact in FP64 (then
+ * every order gives the sequential sum's bits); else the sequential loop. */
+int les_setup_area(int im, int jm, int km, const float *dx1, const float *dy1, const float *dzn,
+                   double *area);
 /* Seeded synthetic scenario: zbm(1:im,1:jm) heightmap and uin/vin/win(1:jm,1:km)
  * inflow planes.  Deterministic for a given seed on every host. */
 int les_scenario_generate(const les_scenario *sc, float *zbm, float *uin, float *vin,
@@ -180,6 +187,12 @@ int les_gpu_download_wait(les_handle *h, long long ticket);
  * constants (les.f95:38-42 delx1, the log-law factor of vel2.f95:138).  Required
  * once before the first solver call and after any later grid upload. */
 int les_gpu_commit_setup(les_handle *h);
+/* feedbfm.f95:87-116 on the device: the b, c, d masks (1 inside a building, where
+ * zbm(i,j) > z2(k) + 0.5*dzn(k), else 0; 0 in the halos) made from the heightmap
+ * zbm(1:im,1:jm) (column-major, i fastest) in place of uploading the three 3-D mask
+ * arrays.  Needs z2 and dzn uploaded first; masks uploaded later change the result
+ * per field as before.  Synchronises the handle's stream. */
+int les_gpu_feedbfm(les_handle *h, const float *zbm);
 /* Convenience: generate the scenario, run the host setup and upload + commit. */
 int les_gpu_setup_scenario(les_handle *h, const les_scenario *sc);
 

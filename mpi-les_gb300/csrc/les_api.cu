@@ -83,6 +83,7 @@ struct les_handle {
   uint8_t *mask_d = nullptr;
   std::vector<uint8_t> mask_h;
   bool mask_dirty = true;
+  bool mask_on_device = false;  // les_gpu_feedbfm wrote mask_d; mask_h is stale
   std::map<int, std::vector<float>> h1d;  // 1-D arrays and inflow planes (host copies)
   float *g1_d = nullptr;                  // 1-D arrays on the device
   float *inflow_d = nullptr;
@@ -343,6 +344,11 @@ extern "C" int les_gpu_upload(les_handle *h, int field, const float *host, const
   }
   if (field >= LES_FIELD_BMASK1 && field <= LES_FIELD_DMASK1) {
     const uint8_t bit = (uint8_t)(1u << (field - LES_FIELD_BMASK1));
+    if (h->mask_on_device) {  // the device holds the masks les_gpu_feedbfm made: start from them
+      CK(h, cudaMemcpyAsync(h->mask_h.data(), h->mask_d, h->nfloat, cudaMemcpyDeviceToHost, h->s));
+      CK(h, cudaStreamSynchronize(h->s));
+      h->mask_on_device = false;
+    }
     for (int k = lb[2]; k <= ub[2]; ++k)
       for (int j = lb[1]; j <= ub[1]; ++j)
         for (int i = lb[0]; i <= ub[0]; ++i) {
@@ -472,6 +478,29 @@ extern "C" int les_gpu_download(les_handle *h, int field, float *host, const int
     if (rc) return rc;
     return download_wait(h, t);
   }
+  if (field >= LES_FIELD_BMASK1 && field <= LES_FIELD_DMASK1) {
+    // the masks as the kernels see them: the device's bits if les_gpu_feedbfm made them
+    // or a commit uploaded them, else the host copy not yet committed
+    const uint8_t bit = (uint8_t)(1u << (field - LES_FIELD_BMASK1));
+    std::vector<uint8_t> dev;
+    const uint8_t *m = h->mask_h.data();
+    if (!h->mask_dirty) {
+      dev.resize(h->nfloat);
+      CK(h, cudaMemcpyAsync(dev.data(), h->mask_d, h->nfloat, cudaMemcpyDeviceToHost, h->s));
+      CK(h, cudaStreamSynchronize(h->s));
+      m = dev.data();
+    }
+    const size_t nx = ub[0] - lb[0] + 1, ny = ub[1] - lb[1] + 1;
+    for (int k = lb[2]; k <= ub[2]; ++k)
+      for (int j = lb[1]; j <= ub[1]; ++j)
+        for (int i = lb[0]; i <= ub[0]; ++i) {
+          const bool in = i >= -LES_IOFF && i < h->pi - LES_IOFF && j >= -LES_JOFF && j < h->nj - LES_JOFF &&
+                          k >= -LES_KOFF && k < h->dims.km + 4 - LES_KOFF;
+          const uint8_t v = in ? m[(size_t)(k + LES_KOFF) * h->np + (size_t)(j + LES_JOFF) * h->pi + (i + LES_IOFF)] : 0;
+          host[(i - lb[0]) + nx * ((j - lb[1]) + ny * (size_t)(k - lb[2]))] = (v & bit) ? 1.f : 0.f;
+        }
+    return LES_OK;
+  }
   if (field == LES_FIELD_DELX1) {
     if (!h->committed) return fail(h, LES_ERR_STATE, "delx1 is derived at commit");
     auto it = h->h1d.find(LES_FIELD_DELX1);
@@ -594,11 +623,12 @@ extern "C" int les_gpu_commit_setup(les_handle *h) {
     CK(h, cudaMemcpyAsync(h->mask_d, h->mask_h.data(), h->nfloat, cudaMemcpyHostToDevice, h->s));
     h->mask_dirty = false;
   }
-  // sum of cell volumes in FP64, sequential in the reference's loop order (press.f95:65-72)
+  // sum of cell volumes in FP64, as summed sequentially in the reference's loop order
+  // (press.f95:65-72)
   double area = 0.0;
-  for (int k = 1; k <= km; ++k)
-    for (int j = 1; j <= jm; ++j)
-      for (int i = 1; i <= im; ++i) area += (double)(dx1(i) * dy1(j) * dzn(k));
+  if (int rc = les_setup_area(im, jm, km, h->h1d[LES_FIELD_DX1].data(), h->h1d[LES_FIELD_DY1].data(),
+                           h->h1d[LES_FIELD_DZN].data(), &area))
+    return fail(h, rc, "commit: les_setup_area failed");
   CK(h, cudaMemcpyAsync(h->scal_d + SC_AREA, &area, sizeof(double), cudaMemcpyHostToDevice, h->s));
   CK(h, cudaStreamSynchronize(h->s));
   // domain view
@@ -651,6 +681,29 @@ extern "C" int les_gpu_commit_setup(les_handle *h) {
   return LES_OK;
 }
 
+extern "C" int les_gpu_feedbfm(les_handle *h, const float *zbm) {
+  if (!h || !zbm) return LES_ERR_ARG;
+  const int im = h->dims.im, jm = h->dims.jm, km = h->dims.km;
+  auto z2 = h->h1d.find(LES_FIELD_Z2), dzn = h->h1d.find(LES_FIELD_DZN);
+  if (z2 == h->h1d.end() || dzn == h->h1d.end())
+    return fail(h, LES_ERR_STATE, "feedbfm: upload z2 and dzn first");
+  // the threshold z2(k) + 0.5*dzn(k) in FP32 on the host, as feedbfm.f95:91 rounds it
+  const size_t nz = (size_t)im * jm;
+  std::vector<float> buf(nz + km);
+  std::copy(zbm, zbm + nz, buf.begin());
+  for (int k = 1; k <= km; ++k) buf[nz + k - 1] = z2->second[k] + 0.5f * dzn->second[k + 1];
+  float *tmp = nullptr;
+  CK(h, cudaMallocAsync((void **)&tmp, buf.size() * sizeof(float), h->s));
+  CK(h, cudaMemcpyAsync(tmp, buf.data(), buf.size() * sizeof(float), cudaMemcpyHostToDevice, h->s));
+  LesCtx c{h->s, &h->nlaunch};
+  les_launch_feedbfm(h->mask_d, tmp, tmp + nz, im, jm, km, h->pi, h->nj, km + 4, c);
+  CK(h, cudaFreeAsync(tmp, h->s));
+  CK(h, cudaStreamSynchronize(h->s));  // buf is freed on return
+  h->mask_dirty = false;
+  h->mask_on_device = true;
+  return check_launch(h, "feedbfm");
+}
+
 extern "C" int les_gpu_setup_scenario(les_handle *h, const les_scenario *sc) {
   if (!h || !sc) return LES_ERR_ARG;
   const int im = h->dims.im, jm = h->dims.jm, km = h->dims.km;
@@ -667,9 +720,6 @@ extern "C" int les_gpu_setup_scenario(les_handle *h, const les_scenario *sc) {
   std::vector<float> zbm((size_t)im * jm), uin((size_t)jm * km), vin((size_t)jm * km), win((size_t)jm * km);
   rc = les_scenario_generate(sc, zbm.data(), uin.data(), vin.data(), win.data());
   if (rc) return fail(h, rc, "les_scenario_generate failed");
-  std::vector<float> dm((size_t)(im + 2) * (jm + 2) * (km + 2));
-  rc = les_setup_masks(im, jm, km, zbm.data(), z2.data(), dzn.data(), nullptr, nullptr, nullptr, dm.data());
-  if (rc) return fail(h, rc, "les_setup_masks failed");
   struct U1 { int id; const float *p; int lo, hi; };
   const U1 ones[] = {{LES_FIELD_DX1, dx1.data(), -1, im + 1}, {LES_FIELD_DY1, dy1.data(), 0, jm + 1},
                      {LES_FIELD_DZN, dzn.data(), -1, km + 2}, {LES_FIELD_DZS, dzs.data(), -1, km + 2},
@@ -686,10 +736,8 @@ extern "C" int les_gpu_setup_scenario(les_handle *h, const les_scenario *sc) {
   if ((rc = les_gpu_upload(h, LES_FIELD_UIN, uin.data(), lbi, ubi))) return rc;
   if ((rc = les_gpu_upload(h, LES_FIELD_VIN, vin.data(), lbi, ubi))) return rc;
   if ((rc = les_gpu_upload(h, LES_FIELD_WIN, win.data(), lbi, ubi))) return rc;
-  // b, c, d masks are equal on the interior (feedbfm.f95:106-116)
-  const int lbm[3] = {0, 0, 0}, ubm[3] = {im + 1, jm + 1, km + 1};
-  for (int f = LES_FIELD_BMASK1; f <= LES_FIELD_DMASK1; ++f)
-    if ((rc = les_gpu_upload(h, f, dm.data(), lbm, ubm))) return rc;
+  // the masks are made on the device from the heightmap (feedbfm.f95:87-116)
+  if ((rc = les_gpu_feedbfm(h, zbm.data()))) return rc;
   return les_gpu_commit_setup(h);
 }
 

@@ -549,6 +549,26 @@ inline unsigned fix_grid(const LesDom &d, dim3 g) {
 }
 inline uint3 u3(dim3 g) { return make_uint3(g.x, g.y, g.z); }
 
+// feedbfm.f95:87-95 sets amask1 = 0 where the building top zbm(i,j) is above the cell
+// centre z2(k) + 0.5*dzn(k); :106-116 set b, c, dmask1 = 1 there.  Every padded cell is
+// written, halos and ground-free cells 0, so the result does not depend on what the
+// mask buffer held.
+__global__ void k_feedbfm(uint8_t *mask, const float *zbm, const float *thr, int im, int jm, int km, int pi, int nj) {
+  const int ip = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  if (ip >= pi) return;
+  const int i = ip - LES_IOFF, j = (int)blockIdx.y - LES_JOFF, k = (int)blockIdx.z - LES_KOFF;
+  uint8_t m = 0;
+  if (i >= 1 && i <= im && j >= 1 && j <= jm && k >= 1 && k <= km)
+    m = zbm[(size_t)(i - 1) + (size_t)(j - 1) * im] > thr[k - 1] ? 7 : 0;
+  mask[((size_t)blockIdx.z * nj + blockIdx.y) * pi + ip] = m;
+}
+
+void les_launch_feedbfm(uint8_t *mask, const float *zbm, const float *thr, int im, int jm, int km, int pi,
+                        int nj, int nk, LesCtx ctx) {
+  k_feedbfm<<<dim3((pi + 127) / 128, nj, nk), 128, 0, ctx.s>>>(mask, zbm, thr, im, jm, km, pi, nj);
+  ++*ctx.nlaunch;
+}
+
 void les_launch_velnw(const LesDom &d, LesCtx ctx) {
   const dim3 g = interior_grid(d, d.km), b(BX, BY);
   LAUNCH(ctx, LES_PZ_SWITCH(d, k_velnw, <<<g, b, 0, ctx.s>>>(d)));

@@ -15,6 +15,11 @@ void les_launch_velnw(const LesDom &d, LesCtx ctx);
 void les_launch_bondv1(const LesDom &d, int n, LesCtx ctx);
 void les_launch_feedbf(const LesDom &d, LesCtx ctx);
 void les_launch_boundsm(const LesDom &d, LesCtx ctx);
+// feedbfm.f95:87-116 on the device: the b, c, d mask bits (1, 2, 4) of every padded cell
+// of a domain with row pitch pi, nj rows per plane and nk planes, from zbm(1:im,1:jm)
+// and thr(k) = z2(k) + 0.5*dzn(k), k = 1..km (thr[k-1])
+void les_launch_feedbfm(uint8_t *mask, const float *zbm, const float *thr, int im, int jm, int km, int pi,
+                        int nj, int nk, LesCtx ctx);
 // les_fused.cu: velfg (optionally with feedbf) and les (optionally with adam)
 void les_launch_velfg_fused(const LesDom &d, bool with_feedbf, LesCtx ctx);
 void les_launch_les_fused(const LesDom &d, bool with_adam, LesCtx ctx);

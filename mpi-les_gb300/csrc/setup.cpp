@@ -147,6 +147,67 @@ extern "C" int les_setup_masks(int im, int jm, int km, const float *zbm, const f
   return LES_OK;
 }
 
+namespace {
+
+// Value of the last bit of a positive normal float.
+double ulp_of(float t) {
+  int e;
+  std::frexp(t, &e);  // t = m * 2^e, m in [0.5, 1)
+  return std::ldexp(1.0, e - 24);
+}
+
+}  // namespace
+
+extern "C" int les_setup_area(int im, int jm, int km, const float *dx1_, const float *dy1_,
+                              const float *dzn_, double *area) {
+  if (im < 1 || jm < 1 || km < 1 || !dx1_ || !dy1_ || !dzn_ || !area) return LES_ERR_ARG;
+  C1 dx1{dx1_, -1}, dy1{dy1_, 0}, dzn{dzn_, -1};
+  // Distinct spacings with their multiplicities: the product dx1(i)*dy1(j)*dzn(k)
+  // depends on i and j only through dx1(i) and dy1(j).
+  auto groups = [](auto get, int n) {
+    std::vector<std::pair<float, double>> g;
+    for (int q = 1; q <= n; ++q) {
+      const float x = get(q);
+      auto it = std::find_if(g.begin(), g.end(), [&](const std::pair<float, double> &e) {
+        return std::memcmp(&e.first, &x, 4) == 0;
+      });
+      if (it == g.end()) {
+        if (g.size() >= 64) return std::vector<std::pair<float, double>>();  // too many: give up
+        g.push_back({x, 1.0});
+      } else {
+        it->second += 1.0;
+      }
+    }
+    return g;
+  };
+  const auto ga = groups([&](int i) { return dx1[i]; }, im);
+  const auto gb = groups([&](int j) { return dy1[j]; }, jm);
+  bool exact = !ga.empty() && !gb.empty();
+  double sum = 0.0, umin = INFINITY;
+  for (int k = 1; k <= km && exact; ++k)
+    for (const auto &a : ga)
+      for (const auto &b : gb) {
+        const float t = a.first * b.first * dzn[k];
+        if (!(t > 0.f) || !std::isfinite(t) || !std::isnormal(t)) { exact = false; break; }
+        umin = std::min(umin, ulp_of(t));
+        // count * t is a sum of equal terms below the bound checked next, so exact
+        sum += (a.second * b.second) * (double)t;
+      }
+  // Every term is a multiple of umin; while the whole sum stays below 2^53 umin every
+  // partial sum, in any order, is a multiple of umin that FP64 holds exactly, so the
+  // grouped sum equals the sequential one.  2^52 leaves room for rounding of `sum`.
+  if (exact && sum <= std::ldexp(umin, 52)) {
+    *area = sum;
+    return LES_OK;
+  }
+  double s = 0.0;
+  for (int k = 1; k <= km; ++k)
+    for (int j = 1; j <= jm; ++j)
+      for (int i = 1; i <= im; ++i) s += (double)(dx1[i] * dy1[j] * dzn[k]);
+  *area = s;
+  return LES_OK;
+}
+
 extern "C" int les_scenario_generate(const les_scenario *sc, float *zbm, float *uin, float *vin,
                                      float *win) {
   if (!sc || !zbm || !uin || !vin || !win) return LES_ERR_ARG;

@@ -174,6 +174,8 @@ def load_library(path: str | None = None) -> C.CDLL:
         "les_gpu_download_async": (C.c_int, [vp, C.c_int, fp_, ip_, ip_, C.POINTER(C.c_longlong)]),
         "les_gpu_download_wait": (C.c_int, [vp, C.c_longlong]),
         "les_gpu_commit_setup": (C.c_int, [vp]),
+        "les_gpu_feedbfm": (C.c_int, [vp, fp_]),
+        "les_setup_area": (C.c_int, [C.c_int] * 3 + [fp_] * 3 + [C.POINTER(C.c_double)]),
         "les_gpu_setup_scenario": (C.c_int, [vp, C.POINTER(LesScenario)]),
         "les_gpu_velnw": (C.c_int, [vp]),
         "les_gpu_bondv1": (C.c_int, [vp, C.c_int]),
@@ -244,6 +246,20 @@ def setup_grid(im, jm, km, dx=4.0, dy=4.0, dz_law=1, dz0=2.0, dz_ratio=1.04):
     if rc:
         raise ValueError(f"les_setup_grid: {ERRORS.get(rc, rc)}")
     return a
+
+
+def setup_area(im: int, jm: int, km: int, dx1, dy1, dzn) -> float:
+    """The FP64 interior volume press divides by (press.f95:65-72), as summed
+    sequentially over k, j, i (dx1(-1:im+1), dy1(0:jm+1), dzn(-1:km+2))."""
+    lib = load_library()
+    a = [np.ascontiguousarray(x, np.float32) for x in (dx1, dy1, dzn)]
+    if (a[0].size, a[1].size, a[2].size) != (im + 3, jm + 2, km + 4):
+        raise ValueError("setup_area: dx1, dy1, dzn must have extents -1:im+1, 0:jm+1, -1:km+2")
+    out = C.c_double(0.0)
+    rc = lib.les_setup_area(im, jm, km, *[_fptr(x) for x in a], C.byref(out))
+    if rc:
+        raise ValueError(f"les_setup_area: {ERRORS.get(rc, rc)}")
+    return out.value
 
 
 def generate_scenario(sc: Scenario):
@@ -371,6 +387,13 @@ class Domain:
 
     def commit(self):
         self._check(self.lib.les_gpu_commit_setup(self._h), "commit_setup")
+
+    def feedbfm(self, zbm: np.ndarray):
+        """feedbfm.f95:87-116 on the device: the b, c, d masks from zbm (im, jm)."""
+        z = np.asfortranarray(zbm, dtype=np.float32)
+        if z.shape != (self.im, self.jm):
+            raise ValueError(f"feedbfm: zbm must have shape {(self.im, self.jm)}")
+        self._check(self.lib.les_gpu_feedbfm(self._h, _fptr(z)), "feedbfm")
 
     def setup_scenario(self, sc: Scenario):
         c = sc.to_c()

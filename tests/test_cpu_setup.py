@@ -116,3 +116,29 @@ def test_direction_rotates_inflow(built_lib):
     sc2 = scenario(40, 32, 20, seed=3, direction_deg=120.0, noise=0.0)
     _, u2, v2, _ = lesgpu.generate_scenario(sc2)
     assert np.allclose(np.degrees(np.arctan2(v2, u2)), 30.0, atol=1e-3)
+
+
+def _area_sequential(im, jm, km, dx1, dy1, dzn):
+    """press.f95:65-72 in FP64: k outer, i inner, each product rounded to FP32."""
+    t = ((dx1[2:im + 2][:, None] * dy1[1:jm + 1][None, :]).astype(np.float32)[:, :, None]
+         * dzn[2:km + 2][None, None, :]).astype(np.float32)
+    s = 0.0
+    for x in np.transpose(t, (2, 1, 0)).astype(np.float64).ravel().tolist():
+        s += x
+    return s
+
+
+@pytest.mark.parametrize("case", ["uniform", "stretched", "steep", "three_dx", "random_dx"])
+def test_setup_area_equals_the_sequential_sum(built_lib, case):
+    im, jm, km = 60, 44, 24
+    g = lesgpu.setup_grid(im, jm, km, dz_law=1, dz0=0.01 if case == "steep" else 2.0,
+                          dz_ratio=1.9 if case == "steep" else (1.0 if case == "uniform" else 1.04))
+    dx1, dy1, dzn = g["dx1"].copy(), g["dy1"].copy(), g["dzn"].copy()
+    rng = np.random.default_rng(3)
+    if case == "three_dx":
+        dx1[:] = rng.choice(np.array([3.0, 4.0, 5.5], np.float32), dx1.size)
+        dy1[:] = rng.choice(np.array([2.0, 3.3], np.float32), dy1.size)
+    if case == "random_dx":
+        dx1[:] = rng.uniform(1.0, 5.0, dx1.size).astype(np.float32)
+    got = lesgpu.setup_area(im, jm, km, dx1, dy1, dzn)
+    assert got == _area_sequential(im, jm, km, dx1, dy1, dzn), case
