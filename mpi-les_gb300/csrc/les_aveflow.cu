@@ -47,12 +47,21 @@ __global__ void k_ave_zero(LesDom d, LesAve A) {
   A.avew[c] = 0.f;
 }
 
-// aveflow.f95:117-149 (n >= n1)
-__global__ void k_ave_acc(LesDom d, LesAve A) {
-  const AveIdx x = ave_idx(d);
-  if (!x.row_w) return;
-  const int c = x.c;
-  if (x.full) {
+// aveflow.f95:117-149 (n >= n1), four cells of a row per thread as float4: cell i0 =
+// 1 + 4t sits at a 16-byte boundary of the padded row (i + 3 = 4t + 4).  Groups that
+// reach past im (the row's last cells, where u and w have different extents) take the
+// per-cell path.
+__device__ __forceinline__ float4 ld4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
+__device__ __forceinline__ void add4(float *p, float4 x) {
+  float4 a = *reinterpret_cast<float4 *>(p);
+  a.x = a.x + x.x; a.y = a.y + x.y; a.z = a.z + x.z; a.w = a.w + x.w;
+  *reinterpret_cast<float4 *>(p) = a;
+}
+__device__ __forceinline__ float4 sq4(float4 x) { return make_float4(x.x * x.x, x.y * x.y, x.z * x.z, x.w * x.w); }
+
+__device__ __forceinline__ void ave_acc_cell(const LesDom &d, const LesAve &A, int i, int c, bool k1) {
+  const bool row_u = i <= d.im, full = row_u && k1;
+  if (full) {
     const float u = d.u[c], v = d.v[c], w = d.w[c], s = d.sm[c];
     A.avev[c] = A.avev[c] + v;
     A.avep[c] = A.avep[c] + d.p[c];
@@ -61,11 +70,43 @@ __global__ void k_ave_acc(LesDom d, LesAve A) {
     A.aveww[c] = A.aveww[c] + w * w;
     A.avesm[c] = A.avesm[c] + s;
     A.avesmsm[c] = A.avesmsm[c] + s * s;
-    const int cd = c - d.np;  // k-1
+    const int cd = c - d.np;
     A.uwfx[c] = A.uwfx[c] + 0.5f * (d.u[cd] + u) * 0.5f * (d.w[cd] + d.w[cd + 1]);
   }
-  if (x.row_u) A.aveu[c] = A.aveu[c] + d.u[c];
+  if (row_u) A.aveu[c] = A.aveu[c] + d.u[c];
   A.avew[c] = A.avew[c] + d.w[c];
+}
+
+__global__ void k_ave_acc4(LesDom d, LesAve A) {
+  const int i0 = 1 + 4 * (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  if (i0 > d.im + 1) return;
+  const int j = (int)blockIdx.y + 1, k = (int)blockIdx.z;
+  const int c = lix(d, i0, j, k);
+  if (i0 + 3 > d.im) {
+    for (int e = 0; e < 4 && i0 + e <= d.im + 1; ++e) ave_acc_cell(d, A, i0 + e, c + e, k >= 1);
+    return;
+  }
+  const float4 u = ld4(d.u + c), w = ld4(d.w + c);
+  add4(A.aveu + c, u);
+  add4(A.avew + c, w);
+  if (k < 1) return;
+  const float4 v = ld4(d.v + c), s = ld4(d.sm + c);
+  add4(A.avev + c, v);
+  add4(A.avep + c, ld4(d.p + c));
+  add4(A.aveuu + c, sq4(u));
+  add4(A.avevv + c, sq4(v));
+  add4(A.aveww + c, sq4(w));
+  add4(A.avesm + c, s);
+  add4(A.avesmsm + c, sq4(s));
+  const int cd = c - d.np;
+  const float4 ud = ld4(d.u + cd), wd = ld4(d.w + cd);
+  const float w4 = d.w[cd + 4];
+  float4 f;
+  f.x = 0.5f * (ud.x + u.x) * 0.5f * (wd.x + wd.y);
+  f.y = 0.5f * (ud.y + u.y) * 0.5f * (wd.y + wd.z);
+  f.z = 0.5f * (ud.z + u.z) * 0.5f * (wd.z + wd.w);
+  f.w = 0.5f * (ud.w + u.w) * 0.5f * (wd.w + w4);
+  add4(A.uwfx + c, f);
 }
 
 // aveflow.f95:151-185 (n == nmax): the divisions
@@ -103,7 +144,8 @@ void les_launch_aveflow(const LesDom &d, const LesAve &A, int n, int n1, int nma
     ++*ctx.nlaunch;
   }
   if (n >= n1) {
-    k_ave_acc<<<g, b, 0, ctx.s>>>(d, A);
+    const int groups = (d.im + 1 + 3) / 4;  // cells 1 .. im+1, four per thread
+    k_ave_acc4<<<dim3((groups + 127) / 128, d.jm, d.km + 1), b, 0, ctx.s>>>(d, A);
     ++*ctx.nlaunch;
   }
   if (n == nmax) {
