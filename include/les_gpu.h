@@ -267,7 +267,7 @@ int les_batch_last_error(les_batch *b, char *buf, size_t len);
  * the squares of u, v, w, sm, sm and the u-w flux; at n == nmax they are divided by
  * nmax-n1+1 and the rms fluctuations and the mean-removed flux formed.  The averaging
  * arrays (11 fields) are allocated on the first call.  The reference's unformatted
- * writes of the averages (data10, data11) are the host's: download the fields. */
+ * writes of the averages at nmax are les_gpu_write_data10/11. */
 int les_gpu_aveflow(les_handle *h, int n, int n1, int nmax);
 
 /* ---- the reference's result and restart files ----------------------------------
@@ -290,6 +290,10 @@ int les_gpu_write_data21(les_handle *h, const char *path, int flags);
 int les_gpu_write_data30(les_handle *h, const char *path, int n, float time, int flags);
 /* anime.f95:492-595: f, g, h, fold, gold, hold */
 int les_gpu_write_data31(les_handle *h, const char *path, int flags);
+/* aveflow.f95:209-263 (n == nmax): aveu, avew, avev -- in that order */
+int les_gpu_write_data10(les_handle *h, const char *path, int flags);
+/* aveflow.f95:273-344 (n == nmax): aveuu, aveww, avevv (the rms values), uwfx */
+int les_gpu_write_data11(les_handle *h, const char *path, int flags);
 /* ifdata_out(n,n0,n1,nmax,time,...) of anime.f95:326, called after every step
  * (main.f95:318): when n == n1-1 or n == nmax it writes <dir>/data30NNNNNN.dat and
  * <dir>/data31NNNNNN.dat (NNNNNN = n as i6.6) and sets *written (may be NULL) to 1;

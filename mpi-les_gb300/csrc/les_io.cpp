@@ -7,6 +7,8 @@
 //   data21             adam.f95:20-27     fold, gold, hold, fghold
 //   data30NNNNNN.dat   anime.f95:370-490  (n, time), then u, v, w, p, usum, vsum, wsum
 //   data31NNNNNN.dat   anime.f95:492-595  f, g, h, fold, gold, hold
+//   data10             aveflow.f95:209-263  aveu, avew, avev       (the time averages at
+//   data11             aveflow.f95:273-344  aveuu, aveww, avevv, uwfx    n == nmax)
 // and the restart reader of ifdata.f95:252-480, which reads data30 and data31 back into
 // the interiors of those 13 fields (halos stay as they were).  On one process the
 // reference's ipmax x jpmax x km box of data30/data31 is im x jm x km.
@@ -173,6 +175,8 @@ const int kData20[] = {LES_FIELD_U, LES_FIELD_V, LES_FIELD_W, LES_FIELD_P,
 const int kData21[] = {LES_FIELD_FOLD, LES_FIELD_GOLD, LES_FIELD_HOLD, 0 /* fghold */};
 const int kData31[] = {LES_FIELD_F, LES_FIELD_G, LES_FIELD_H,
                        LES_FIELD_FOLD, LES_FIELD_GOLD, LES_FIELD_HOLD};
+const int kData10[] = {LES_FIELD_AVEU, LES_FIELD_AVEW, LES_FIELD_AVEV};
+const int kData11[] = {LES_FIELD_AVEUU, LES_FIELD_AVEWW, LES_FIELD_AVEVV, LES_FIELD_UWFX};
 
 int write_file(les_handle *h, const char *path, int flags, const int *fields, int nfields,
                const int *head_n, const float *head_time) {
@@ -317,6 +321,16 @@ extern "C" int les_gpu_write_data30(les_handle *h, const char *path, int n, floa
 extern "C" int les_gpu_write_data31(les_handle *h, const char *path, int flags) {
   if (!h) return LES_ERR_ARG;
   return write_file(h, path, flags, kData31, 6, nullptr, nullptr);
+}
+
+extern "C" int les_gpu_write_data10(les_handle *h, const char *path, int flags) {
+  if (!h) return LES_ERR_ARG;
+  return write_file(h, path, flags, kData10, 3, nullptr, nullptr);
+}
+
+extern "C" int les_gpu_write_data11(les_handle *h, const char *path, int flags) {
+  if (!h) return LES_ERR_ARG;
+  return write_file(h, path, flags, kData11, 4, nullptr, nullptr);
 }
 
 extern "C" int les_gpu_ifdata_out(les_handle *h, const char *dir, int n, int n1, int nmax, float time, int flags,

@@ -32,7 +32,7 @@ module module_LES_gpu
   private
   public :: initialise_LES_gpu, run_LES_gpu, sync_LES_gpu, finalise_LES_gpu
   public :: velnw, bondv1, velfg, feedbf, les, adam, press, boundp1, boundp2
-  public :: ifdata_out, read_restart_LES_gpu
+  public :: ifdata_out, read_restart_LES_gpu, aveflow
 
   ! field ids of include/les_gpu.h
   integer(c_int), parameter :: LES_FIELD_U = 1, LES_FIELD_V = 2, LES_FIELD_W = 3, LES_FIELD_P = 4
@@ -102,6 +102,18 @@ module module_LES_gpu
       integer(c_int), value :: n, n1, nmax
     end function
     integer(c_int) function les_gpu_write_data20(h, path, flags) bind(C, name='les_gpu_write_data20')
+      import :: c_int, c_ptr, c_char
+      type(c_ptr), value :: h
+      character(kind=c_char), dimension(*) :: path
+      integer(c_int), value :: flags
+    end function
+    integer(c_int) function les_gpu_write_data10(h, path, flags) bind(C, name='les_gpu_write_data10')
+      import :: c_int, c_ptr, c_char
+      type(c_ptr), value :: h
+      character(kind=c_char), dimension(*) :: path
+      integer(c_int), value :: flags
+    end function
+    integer(c_int) function les_gpu_write_data11(h, path, flags) bind(C, name='les_gpu_write_data11')
       import :: c_int, c_ptr, c_char
       type(c_ptr), value :: h
       character(kind=c_char), dimension(*) :: path
@@ -403,6 +415,24 @@ contains
       call check(les_gpu_write_data20(les_h, trim(data20)//c_null_char, 0_c_int), 'press: data20')
     end if
 #endif
+  end subroutine
+
+  ! aveflow of aveflow.f95:5 (called after every step, main.f95:320): the averages stay on
+  ! the device; at n == nmax data10 and data11 are written from them (aveflow.f95:209-344).
+  subroutine aveflow(n, n1, km, jm, im, aveu, avev, avew, avep, avel, aveuu, avevv, aveww, &
+                     avesm, avesmsm, uwfx, avesu, avesv, avesw, avesuu, avesvv, avesww, u, v, w, p, sm, &
+                     nmax, uwfxs, data10, time, data11, data13, data14, amask1)
+    integer, intent(in) :: n, n1, km, jm, im, nmax
+    real, intent(in) :: time
+    character(len=*) :: data10, data11, data13, data14
+    real(4) :: aveu(*), avev(*), avew(*), avep(*), avel(*), aveuu(*), avevv(*), aveww(*)
+    real(4) :: avesm(*), avesmsm(*), uwfx(*), avesu(*), avesv(*), avesw(*), avesuu(*), avesvv(*)
+    real(4) :: avesww(*), u(*), v(*), w(*), p(*), sm(*), uwfxs(*), amask1(*)
+    call check(les_gpu_aveflow(les_h, int(n, c_int), int(n1, c_int), int(nmax, c_int)), 'aveflow')
+    if (n == nmax) then
+      call check(les_gpu_write_data10(les_h, trim(data10)//c_null_char, 0_c_int), 'aveflow: data10')
+      call check(les_gpu_write_data11(les_h, trim(data11)//c_null_char, 0_c_int), 'aveflow: data11')
+    end if
   end subroutine
 
   ! ifdata_out of anime.f95:326 (called after every step, main.f95:318): data30NNNNNN.dat

@@ -10,6 +10,8 @@ data20              press.f95:205-216           u, v, w, p, usum, vsum, wsum
 data21              adam.f95:20-27              fold, gold, hold, fghold
 data30NNNNNN.dat    anime.f95:370-490           (n, time), u, v, w, p, usum, vsum, wsum
 data31NNNNNN.dat    anime.f95:492-595           f, g, h, fold, gold, hold
+data10              aveflow.f95:209-263         aveu, avew, avev
+data11              aveflow.f95:273-344         aveuu, aveww, avevv, uwfx
 ==================  ==========================  =============================================
 
 Every 3-D record is the box (1:im, 1:jm, 1:km) with i fastest: here a
@@ -38,6 +40,8 @@ DATA20 = ("u", "v", "w", "p", "usum", "vsum", "wsum")
 DATA21 = ("fold", "gold", "hold", "fghold")
 DATA30 = DATA20
 DATA31 = ("f", "g", "h", "fold", "gold", "hold")
+DATA10 = ("aveu", "avew", "avev")
+DATA11 = ("aveuu", "aveww", "avevv", "uwfx")
 
 
 def write_records(path: str, records, big_endian: bool = True, max_subrecord: int = MAX_SUBRECORD) -> None:

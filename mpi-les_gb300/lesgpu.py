@@ -207,6 +207,8 @@ def load_library(path: str | None = None) -> C.CDLL:
         "les_gpu_write_data21": (C.c_int, [vp, C.c_char_p, C.c_int]),
         "les_gpu_write_data30": (C.c_int, [vp, C.c_char_p, C.c_int, C.c_float, C.c_int]),
         "les_gpu_write_data31": (C.c_int, [vp, C.c_char_p, C.c_int]),
+        "les_gpu_write_data10": (C.c_int, [vp, C.c_char_p, C.c_int]),
+        "les_gpu_write_data11": (C.c_int, [vp, C.c_char_p, C.c_int]),
         "les_gpu_ifdata_out": (C.c_int, [vp, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_float, C.c_int, ip_]),
         "les_gpu_read_restart": (C.c_int, [vp, C.c_char_p, C.c_char_p, ip_, fp_]),
         "les_batch_create": (C.c_int, [C.POINTER(vp)]),
@@ -485,6 +487,16 @@ class Domain:
         """data31 of anime.f95:492-595: f, g, h, fold, gold, hold."""
         self._check(self.lib.les_gpu_write_data31(self._h, os.fsencode(path), self._io_flags(big_endian)),
                     "write_data31")
+
+    def write_data10(self, path: str, big_endian: bool = True) -> None:
+        """data10 of aveflow.f95:209-263 (aveu, avew, avev), after aveflow at nmax."""
+        self._check(self.lib.les_gpu_write_data10(self._h, os.fsencode(path), self._io_flags(big_endian)),
+                    "write_data10")
+
+    def write_data11(self, path: str, big_endian: bool = True) -> None:
+        """data11 of aveflow.f95:273-344 (aveuu, aveww, avevv, uwfx), after aveflow at nmax."""
+        self._check(self.lib.les_gpu_write_data11(self._h, os.fsencode(path), self._io_flags(big_endian)),
+                    "write_data11")
 
     def ifdata_out(self, directory: str, n: int, n1: int, nmax: int, time: float,
                    big_endian: bool = True) -> bool:

@@ -66,3 +66,31 @@ def test_aveflow_fields_need_a_first_call(built_lib):
         d.aveflow(1, 3, 2)  # nmax < n1
     d.aveflow(1, 1, 1)
     assert d.download(lesgpu.AVEW).shape == (sc.im + 1, sc.jm, sc.km + 3)
+
+
+def test_data10_data11_hold_the_averages(built_lib, tmp_path):
+    """aveflow.f95:209-344: the files written at nmax, record by record, and byte for
+    byte what the independent numpy writer makes of the downloaded averages."""
+    import ftnio
+    sc = scenario(33, 20, 10, seed=204)
+    shape = (sc.im, sc.jm, sc.km)
+    gpu = make_gpu(sc, lesgpu.Params(nmaxp=10))
+    nmax = 4
+    for n in range(1, nmax + 1):
+        gpu.step(n, nmax)
+        gpu.aveflow(n, 2, nmax)
+    ids = {"aveu": lesgpu.AVEU, "avew": lesgpu.AVEW, "avev": lesgpu.AVEV, "aveuu": lesgpu.AVEUU,
+           "aveww": lesgpu.AVEWW, "avevv": lesgpu.AVEVV, "uwfx": lesgpu.UWFX}
+    for name, write, names in (("data10", gpu.write_data10, ftnio.DATA10), ("data11", gpu.write_data11, ftnio.DATA11)):
+        p = str(tmp_path / name)
+        write(p)
+        want = {nm: gpu.download(ids[nm], (1, 1, 1), shape) for nm in names}
+        got, _, _ = ftnio.read_fields(p, names, shape)
+        for nm in names:
+            assert np.array_equal(got[nm].view(np.uint32), want[nm].view(np.uint32)), (name, nm)
+        q = p + ".np"
+        ftnio.write_fields(q, want, names)
+        assert open(p, "rb").read() == open(q, "rb").read(), name
+    fresh = make_gpu(sc, lesgpu.Params())
+    with pytest.raises(lesgpu.LesError, match="aveflow"):
+        fresh.write_data10(str(tmp_path / "none"))
