@@ -168,8 +168,7 @@ def cpu_baseline_sample(threads: int | None = None, im=150, jm=150, km=90, steps
     from oracle import ref as oref
     sc = scenario(seed=1, im=im, jm=jm, km=km)
     zbm, uin, vin, win = lesgpu.generate_scenario(sc)
-    if threads:
-        os.environ["OMP_NUM_THREADS"] = str(threads)
+    used = oref.set_threads(threads or (os.cpu_count() or 1))
     r = oref.Ref(4, im, jm, km, zbm, uin, vin, win, sqrt_half=0, red64=0, fast=True)
     r.step(1, steps + 1)  # warm-up (n == 1 fill)
     t0 = time.perf_counter()
@@ -177,7 +176,7 @@ def cpu_baseline_sample(threads: int | None = None, im=150, jm=150, km=90, steps
         r.step(n, steps + 1)
     dt = time.perf_counter() - t0
     r.close()
-    return im * jm * km * steps / dt, f"{steps} steps of {im}x{jm}x{km} after 1 warm-up step, {dt:.1f} s"
+    return im * jm * km * steps / dt, f"{steps} steps of {im}x{jm}x{km} after 1 warm-up step, {dt:.1f} s", used
 
 
 def run_reference(args):
@@ -187,8 +186,7 @@ def run_reference(args):
     from oracle import ref as oref
     oref.build()
     import lesgpu
-    threads = os.cpu_count() or 1
-    os.environ["OMP_NUM_THREADS"] = str(threads)
+    threads = oref.set_threads(os.cpu_count() or 1)
     # one "step" = one oracle time step on a 300x300x90 sample of the workload's domain
     im, jm, km = 300, 300, 90
     sc = scenario(seed=1, im=im, jm=jm, km=km)
@@ -415,8 +413,8 @@ def run_ours(args):
         cpu = None
         if not args.no_cpu:
             try:
-                cv, sample = cpu_baseline_sample(threads=1)
-                cpu = {"value": cv, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample}
+                cv, sample, used = cpu_baseline_sample(threads=1)
+                cpu = {"value": cv, "unit": UNIT, "cores": used, "kind": "port", "sample": sample}
             except Exception as e:  # the baseline must not sink the GPU line
                 cpu = {"value": None, "unit": UNIT, "cores": 1, "kind": "port", "sample": f"failed: {e}"}
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -444,11 +442,11 @@ def run_ours(args):
 def _oracle_check(job):
     """FP64 oracle run of one served scenario (runs in a spawned worker process)."""
     sc_kw, nsteps, gpu_fields = job
-    os.environ.setdefault("OMP_NUM_THREADS", "2")
     import numpy as np
 
     import lesgpu
     from oracle import ref as oref
+    oref.set_threads(2)
     sc = lesgpu.Scenario(**sc_kw)
     zbm, uin, vin, win = lesgpu.generate_scenario(sc)
     r = oref.Ref(8, sc.im, sc.jm, sc.km, zbm, uin, vin, win, dx=sc.dx, dy=sc.dy, dz_law=sc.dz_law, dz0=sc.dz0,

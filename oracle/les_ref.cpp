@@ -24,6 +24,9 @@
 #include <cstring>
 #include <string>
 #include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 namespace {
 
@@ -1246,5 +1249,15 @@ int ref_bounds_checked(void) {
 }
 
 const char *ref_last_error(void) { return g_err.c_str(); }
+
+int ref_set_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+  return omp_get_max_threads();
+#else
+  (void)n;
+  return 1;
+#endif
+}
 
 }  // extern "C"

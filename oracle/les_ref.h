@@ -67,6 +67,9 @@ void ref_diag(void *h, double *out);
 /* 1 if built with array bounds checks (mirrors gfortran -fbounds-check) */
 int ref_bounds_checked(void);
 const char *ref_last_error(void);
+/* threads of the fast build's parallel loops from now on (n > 0), for the calling
+ * thread; returns the number its next loops will use (1 in the serial builds) */
+int ref_set_threads(int n);
 
 #ifdef __cplusplus
 }

@@ -55,8 +55,17 @@ def load(fast: bool = False) -> C.CDLL:
     lib.ref_diag.argtypes = [vp, dp]
     lib.ref_bounds_checked.restype = C.c_int
     lib.ref_last_error.restype = C.c_char_p
+    lib.ref_set_threads.restype = C.c_int
+    lib.ref_set_threads.argtypes = [C.c_int]
     _libs[name] = lib
     return lib
+
+
+def set_threads(n: int, fast: bool = True) -> int:
+    """Threads of the fast build's parallel loops (OMP_NUM_THREADS is read once, when
+    the OpenMP runtime starts -- often at `import torch` -- so it cannot be relied on);
+    returns the count the next steps use."""
+    return int(load(fast).ref_set_threads(int(n)))
 
 
 class Ref:
