@@ -214,3 +214,31 @@ def test_steps_vs_committed_golden(built_lib):
             e = rel_err(x, g[f"{nm}{prec}"].astype(np.float64))
             assert e <= 1e-4, (nm, prec, e)
     assert gpu.diag()["iters"] == int(g["diag32"][0])
+
+
+@pytest.mark.parametrize("pjuge,lo,hi", [(12000.0, 2, 48), (40000.0, 1, 6)])
+def test_sor_early_exit_like_the_reference(built_lib, pjuge, lo, hi):
+    """press.f95:119-121: the SOR loop exits once sor < pjuge.  With thresholds the
+    residual crosses mid-loop (and after the first iteration), the whole-step graph
+    and the per-subroutine calls stop at the oracle's iteration in every step."""
+    sc = scenario(40, 24, 12, seed=5)
+    params = lesgpu.Params(sor_fixed=0, pjuge=pjuge)
+    gpu = make_gpu(sc, params)
+    stages = make_gpu(sc, params)
+    orc = make_ref(4, sc, params, sqrt_half=1, red64=1)
+    iters = []
+    for n in range(1, 6):
+        gpu.step(n, 5)
+        stages.velnw(); stages.bondv1(n); stages.velfg(); stages.feedbf(); stages.les(); stages.adam()
+        stages.press(n, 5)
+        orc.step(n, 5)
+        want = orc.diag()["iters"]
+        assert gpu.diag()["iters"] == want, (n, gpu.diag(), orc.diag())
+        assert stages.diag()["iters"] == want, (n, stages.diag(), orc.diag())
+        iters.append(want)
+    assert lo <= min(iters) and max(iters) <= hi, iters
+    for fid, nm in FIELDS:
+        e = rel_err(_interior(gpu, fid, sc, True), _interior(orc, fid, sc, False))
+        assert e <= 1e-5, (nm, e)
+        x, y = gpu.download(fid), stages.download(fid)
+        assert np.array_equal(x.view(np.uint32), y.view(np.uint32)), nm
