@@ -171,12 +171,22 @@ def cpu_baseline_sample(threads: int | None = None, im=150, jm=150, km=90, steps
     used = oref.set_threads(threads or (os.cpu_count() or 1))
     r = oref.Ref(4, im, jm, km, zbm, uin, vin, win, sqrt_half=0, red64=0, fast=True)
     r.step(1, steps + 1)  # warm-up (n == 1 fill)
+    # the step's seven subroutines in main.f95's order, each timed (oracle's step() is
+    # exactly this sequence)
+    order = (("velnw", oref.VELNW), ("bondv1", oref.BONDV1), ("velfg", oref.VELFG), ("feedbf", oref.FEEDBF),
+             ("les", oref.LES), ("adam", oref.ADAM), ("press", oref.PRESS))
+    per = {nm: 0.0 for nm, _ in order}
     t0 = time.perf_counter()
     for n in range(2, steps + 2):
-        r.step(n, steps + 1)
+        for nm, st in order:
+            ts = time.perf_counter()
+            r.stage(st, n, steps + 1)
+            per[nm] += time.perf_counter() - ts
     dt = time.perf_counter() - t0
     r.close()
-    return im * jm * km * steps / dt, f"{steps} steps of {im}x{jm}x{km} after 1 warm-up step, {dt:.1f} s", used
+    per_step = {nm: round(v / steps, 6) for nm, v in per.items()}
+    return (im * jm * km * steps / dt, f"{steps} steps of {im}x{jm}x{km} after 1 warm-up step, {dt:.1f} s", used,
+            per_step)
 
 
 def run_reference(args):
@@ -394,6 +404,10 @@ def run_ours(args):
     # ---- dominant kernel: one SOR iteration, timed alone ----------------------------
     reps = 100
     sor_ms = dom.profile(lesgpu.PROF_SOR, reps)
+    # the other passes of the step, each timed alone with CUDA events on the handle's stream
+    stage_ms = {"velnw": dom.profile(lesgpu.PROF_VELNW, 20), "velfg+feedbf": dom.profile(lesgpu.PROF_VELFG, 20),
+                "les+adam": dom.profile(lesgpu.PROF_LES, 20), "sor_iteration": sor_ms,
+                "step": dom.profile(lesgpu.PROF_STEP, 10)}
     peak, peak_kind = read_peaks()
     alg = SOR_BYTES_PER_CELL_ITER * cells
     achieved = alg / (sor_ms / 1e3) / 1e9
@@ -404,6 +418,7 @@ def run_ours(args):
                 "alg_bytes_per_launch": alg,
                 "sor_tile": {"nx": sor_shape[0], "ny": sor_shape[1], "kchunk": sor_shape[2],
                              "tuner_us": sor_tuned_us},
+                "stages_ms": stage_ms,
                 "step_alg_GBps": BYTES_PER_CELL_STEP * cells / (ms / args.steps / 1e3) / 1e9,
                 "step_frac": BYTES_PER_CELL_STEP * cells / (ms / args.steps / 1e3) / 1e9 / peak}
     dom.close()
@@ -413,8 +428,9 @@ def run_ours(args):
         cpu = None
         if not args.no_cpu:
             try:
-                cv, sample, used = cpu_baseline_sample(threads=1)
-                cpu = {"value": cv, "unit": UNIT, "cores": used, "kind": "port", "sample": sample}
+                cv, sample, used, per_step = cpu_baseline_sample(threads=1)
+                cpu = {"value": cv, "unit": UNIT, "cores": used, "kind": "port", "sample": sample,
+                       "stage_s_per_step": per_step}
             except Exception as e:  # the baseline must not sink the GPU line
                 cpu = {"value": None, "unit": UNIT, "cores": 1, "kind": "port", "sample": f"failed: {e}"}
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
