@@ -402,6 +402,23 @@ __global__ void k_pack_box(const float *__restrict__ src, float *__restrict__ ds
   for (int i = threadIdx.x; i < nx; i += blockDim.x) o[i] = s[i];
 }
 
+// k_pack_box for boxes whose rows start on 16-byte words at both ends (i0 + 3 a multiple
+// of 4, nx a multiple of 4): float4 copies, PACK_ROWS rows per block, one float4 of a
+// row per thread.
+constexpr int PACK_ROWS = 8;
+__global__ void k_pack_box4(const float4 *__restrict__ src, float4 *__restrict__ dst, int pi4, int nj, int i04,
+                            int j0, int k0, int nx4, int ny, int rows) {
+  const int c = threadIdx.x;
+  if (c >= nx4) return;
+#pragma unroll
+  for (int q = 0; q < PACK_ROWS; ++q) {
+    const int row = blockIdx.x * PACK_ROWS + q;  // (j - j0) + ny * (k - k0)
+    if (row >= rows) return;
+    const int jj = row % ny, kk = row / ny;
+    dst[(size_t)row * nx4 + c] = src[((size_t)(k0 + kk + LES_KOFF) * nj + (j0 + jj + LES_JOFF)) * pi4 + i04 + c];
+  }
+}
+
 // Snapshot the box on h->s and queue its copy to `host` on the copy stream.
 int download_async(les_handle *h, int field, float *host, const int lb[3], const int ub[3], long long *ticket) {
   const int nx = ub[0] - lb[0] + 1, ny = ub[1] - lb[1] + 1, nz = ub[2] - lb[2] + 1;
@@ -425,7 +442,14 @@ int download_async(les_handle *h, int field, float *host, const int lb[3], const
   const unsigned rows = (unsigned)ny * (unsigned)nz;
   if (rows > 0) {
     const float *src = is_ave(field) ? h->ave_d[field - LES_FIELD_AVEU] : h->fields[field - 1];
-    k_pack_box<<<rows, 128, 0, h->s>>>(src, sl.buf, h->pi, h->nj, lb[0], lb[1], lb[2], nx, ny);
+    if ((lb[0] + LES_IOFF) % 4 == 0 && nx % 4 == 0 && nx / 4 <= 1024) {
+      const int nx4 = nx / 4, threads = (nx4 + 31) / 32 * 32;
+      k_pack_box4<<<(rows + PACK_ROWS - 1) / PACK_ROWS, threads, 0, h->s>>>(
+          reinterpret_cast<const float4 *>(src), reinterpret_cast<float4 *>(sl.buf), h->pi / 4, h->nj,
+          (lb[0] + LES_IOFF) / 4, lb[1], lb[2], nx4, ny, (int)rows);
+    } else {
+      k_pack_box<<<rows, 128, 0, h->s>>>(src, sl.buf, h->pi, h->nj, lb[0], lb[1], lb[2], nx, ny);
+    }
     CK(h, cudaGetLastError());
   }
   CK(h, cudaEventRecord(sl.packed, h->s));

@@ -73,3 +73,24 @@ def test_async_download_rejects_bad_input(built_lib):
         d._check(d.lib.les_gpu_download_async(d._h, lesgpu.DX1, lesgpu._fptr(np.zeros(30, np.float32)),
                                               lesgpu._iarr((-1, 0, 0)), lesgpu._iarr((20, 0, 0)),
                                               lesgpu.C.byref(lesgpu.C.c_longlong())), "download_async")
+
+
+@pytest.mark.parametrize("shape", [(48, 30, 14), (37, 9, 5)])
+def test_download_boxes_equal_the_uploaded_array(built_lib, shape):
+    """Every box shape: rows starting on a 16-byte word of the padded row with a width
+    that is a multiple of 4 (the float4 pack) and all the others (the scalar pack)."""
+    sc = scenario(*shape, seed=105)
+    d = make_gpu(sc, lesgpu.Params())
+    rng = np.random.default_rng(9)
+    for fid in (lesgpu.U, lesgpu.P, lesgpu.SM):
+        lb, ub = lesgpu.declared_extents(fid, sc.im, sc.jm, sc.km)
+        full = np.asfortranarray(rng.standard_normal(tuple(ub[q] - lb[q] + 1 for q in range(3))).astype(np.float32))
+        d.upload(fid, full)
+        for i0, i1 in ((1, 4), (1, 8), (1, sc.im), (1, sc.im - 1), (2, 9), (max(lb[0], -3), ub[0]), (5, 12)):
+            i0, i1 = max(i0, lb[0]), min(i1, ub[0])
+            if i1 < i0:
+                continue
+            for (j0, j1), (k0, k1) in ((((lb[1], ub[1])), (lb[2], ub[2])), ((2, 3), (1, 2))):
+                got = d.download(fid, (i0, j0, k0), (i1, j1, k1))
+                want = full[i0 - lb[0]:i1 - lb[0] + 1, j0 - lb[1]:j1 - lb[1] + 1, k0 - lb[2]:k1 - lb[2] + 1]
+                assert np.array_equal(got, want), (fid, (i0, j0, k0), (i1, j1, k1))
