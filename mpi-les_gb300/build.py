@@ -18,6 +18,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "liblesgpu.so")
+MAIN = os.path.join(OUT, "les_main")  # the main.f95 time loop on the library (host/les_main.cpp)
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [
@@ -79,6 +80,12 @@ def build(verbose: bool = False, force: bool = False, extra_nvcc: list[str] | No
         tmp = LIB + ".tmp"
         logs.append(_run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart_static", "-lrt", "-ldl", "-lpthread"]))
         os.replace(tmp, LIB)
+    src_main = os.path.join(HERE, "host", "les_main.cpp")
+    if force or _stale(MAIN, [src_main, LIB, os.path.join(HERE, "..", "include", "les_gpu.h")]):
+        tmp = MAIN + ".tmp"
+        logs.append(_run(["g++"] + CXX_FLAGS + ["-I", os.path.join(HERE, "..", "include"), src_main, "-o", tmp,
+                          "-L", OUT, "-llesgpu", "-Wl,-rpath,$ORIGIN"]))
+        os.replace(tmp, MAIN)
     if verbose:
         for lg in logs:
             if lg.strip():

@@ -142,3 +142,18 @@ def test_setup_area_equals_the_sequential_sum(built_lib, case):
         dx1[:] = rng.uniform(1.0, 5.0, dx1.size).astype(np.float32)
     got = lesgpu.setup_area(im, jm, km, dx1, dy1, dzn)
     assert got == _area_sequential(im, jm, km, dx1, dy1, dzn), case
+
+
+def test_les_main_builds_and_refuses_to_run_without_a_gpu(built_lib, tmp_path):
+    """The C++ main program is built beside the library; with no GPU it stops with
+    status 1 and says why (no CPU fallback)."""
+    import subprocess
+    main = os.path.join(os.path.dirname(built_lib), "les_main")
+    r = subprocess.run([main, "--help"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and "usage: les_main" in r.stdout
+    r = subprocess.run([main, "--dims", "bad"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 2
+    r = subprocess.run([main, "--dims", "24x16x8", "--nmax", "2", "--out", str(tmp_path / "d"), "--quiet"],
+                       capture_output=True, text=True, timeout=300)
+    if r.returncode != 0:  # no GPU here
+        assert r.returncode == 1 and "les_gpu_create" in r.stderr, r.stderr
