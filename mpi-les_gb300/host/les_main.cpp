@@ -224,7 +224,8 @@ int main(int argc, char **argv) {
   const double cells = (double)o.im * o.jm * o.km, steps = o.nmax - o.n0 + 1;
   if (o.per_stage && !o.quiet)
     for (int s = 0; s < 7; ++s)
-      std::printf("Time for state %2d = %8.4f s  (%s, per step)\n", s + 1, stage_s[s] / steps, kStage[s]);
+      std::printf("Time for state %2d = %9.3f ms  (%s, per step, with a synchronisation)\n", s + 1,
+                  1e3 * stage_s[s] / steps, kStage[s]);
   std::printf("les_main: %d steps of %d x %d x %d in %.3f s, %.4g cell-steps/s (output included); "
               "last press: %d SOR iterations, residual %.6g; non-finite values: %lld\n",
               (int)steps, o.im, o.jm, o.km, wall, cells * steps / wall, (int)diag[0], diag[1], bad);
