@@ -238,3 +238,25 @@ def test_stages_all_blocks_deferred(built_lib, stage):
             _assert_same_nan(gpu, orc, (lesgpu.RHS,), "press rhs")
         return
     _assert_same_nan(gpu, orc, STATE, stage)
+
+
+@pytest.mark.parametrize("spacing", SPACINGS)
+def test_wall_at_rest_gives_nan_like_the_reference(built_lib, spacing):
+    """vel2.f95:138,173 divide by the wall speed uspd (vspd): where u = v = 0 on the
+    first level the reference forms 0/0, a NaN that les and press then carry.  The GPU
+    reproduces it where the reference does, through velfg, les and a whole step."""
+    sc = scenario(32, 16, 8, seed=57, dx=spacing[0], dy=spacing[1])
+    params = lesgpu.Params(nmaxp=3)
+    gpu = make_gpu(sc, params)
+    orc = make_ref(4, sc, params, sqrt_half=1, red64=1)
+    st = random_state(sc, seed=157)
+    for fid in (lesgpu.U, lesgpu.V):  # at rest on k = 1 over a patch (and its neighbours)
+        st[fid][8:15, 5:11, 1] = 0.0
+    load_state(gpu, orc, st)
+    gpu.velfg(); orc.stage(ref.VELFG)
+    f = gpu.download(lesgpu.F)
+    assert np.isnan(f).any(), "the 0/0 of the wall function did not appear"
+    _assert_same_nan(gpu, orc, (lesgpu.F, lesgpu.G, lesgpu.H), "velfg")
+    gpu.les(); orc.stage(ref.LES)
+    _assert_same_nan(gpu, orc, (lesgpu.F, lesgpu.G, lesgpu.H, lesgpu.SM), "les")
+    assert gpu.nonfinite() == 0  # u, v, w, p are still finite before velnw/press use f
