@@ -682,6 +682,10 @@ extern "C" int les_gpu_commit_setup(les_handle *h) {
     for (int j = 0; j <= jm + 1 && ok; ++j) ok = (dy1(j) == Q);
     for (int j = 0; j <= jm && ok; ++j) ok = (dys(j) == Q);
     d.xy_pow2 = ok ? 1 : 0;
+    // the uniform spacings the P2 kernels use in place of the arrays' (equal) entries
+    d.hx = ok ? P : 0.f; d.hy = ok ? Q : 0.f;
+    d.rhx = ok ? 1.f / P : 0.f; d.rhx2 = ok ? 1.f / (P + P) : 0.f;
+    d.rhy = ok ? 1.f / Q : 0.f; d.rhy2 = ok ? 1.f / (Q + Q) : 0.f;
   }
   {  // every divisor in [2^-20, 2^20]: reciprocal-corrected divisions (dvz)
     auto inr = [](float x) { const float a = std::fabs(x); return std::isfinite(x) && a >= 0x1p-20f && a <= 0x1p20f; };

@@ -80,6 +80,8 @@ struct LesDom {
   int xy_pow2;
   int zfast;
   float rro, rdt, rlogz;
+  // with xy_pow2: the one x spacing hx and y spacing hy, 1/hx, 1/(2 hx), 1/hy, 1/(2 hy)
+  float hx, hy, rhx, rhx2, rhy, rhy2;
   // deferred-block lists of the kernels that use dvz (FIX_*): [0] count, [1] ticket of
   // the fixup kernel, then the linear ids of the blocks left to the fixup kernel
   int *fix[4];
@@ -145,6 +147,21 @@ template <bool P2, bool ZF>
 __device__ __forceinline__ float dvs(float x, float den, float rden, unsigned &bad) {
   return P2 ? x * rden : dvz<ZF>(x, den, rden, bad);
 }
+
+// The x and y spacings and their reciprocals as the kernels read them: dx1(i), dxs(i),
+// 1/dx1(i), 1/(dx1(i)+dx1(i+1)), 1/dxs(i) and the same in y.  With P2 every x and y
+// spacing is one power of two (checked at set-up), so these are the domain's uniform
+// values -- the numbers the arrays hold -- and cost no loads.
+template <bool P2> __device__ __forceinline__ float sx1(const LesDom &d, int i) { return P2 ? d.hx : d.gr.dx1[i]; }
+template <bool P2> __device__ __forceinline__ float sy1(const LesDom &d, int j) { return P2 ? d.hy : d.gr.dy1[j]; }
+template <bool P2> __device__ __forceinline__ float sxs(const LesDom &d, int i) { return P2 ? d.hx : d.gr.dxs[i]; }
+template <bool P2> __device__ __forceinline__ float sys(const LesDom &d, int j) { return P2 ? d.hy : d.gr.dys[j]; }
+template <bool P2> __device__ __forceinline__ float rx1(const LesDom &d, int i) { return P2 ? d.rhx : d.gr.rdx1[i]; }
+template <bool P2> __device__ __forceinline__ float rx1s(const LesDom &d, int i) { return P2 ? d.rhx2 : d.gr.rdx1s[i]; }
+template <bool P2> __device__ __forceinline__ float rxs(const LesDom &d, int i) { return P2 ? d.rhx : d.gr.rdxs[i]; }
+template <bool P2> __device__ __forceinline__ float ry1(const LesDom &d, int j) { return P2 ? d.rhy : d.gr.rdy1[j]; }
+template <bool P2> __device__ __forceinline__ float ry1s(const LesDom &d, int j) { return P2 ? d.rhy2 : d.gr.rdy1s[j]; }
+template <bool P2> __device__ __forceinline__ float rys(const LesDom &d, int j) { return P2 ? d.rhy : d.gr.rdys[j]; }
 
 // Block-level deferral.  A block in which some thread met a dividend outside dvz's range
 // stores nothing; thread 0 appends the block's linear id to `list`, and a fixup kernel

@@ -73,34 +73,42 @@ __device__ __forceinline__ FRaw fload(const LesDom &d, int i, int j, int k) {
 // diu3 and diu6 at k = 1 are the log-law wall gradients, stored by k_wall before velfg runs
 template <int N, bool P2, bool ZF>
 __device__ __forceinline__ NouDiu fcomp(const LesDom &d, const FRaw &r, int i, int j, int k, unsigned &bd) {
-  const float *dx1 = d.gr.dx1, *dy1 = d.gr.dy1, *dzn = d.gr.dzn;
+  const float *dzn = d.gr.dzn;
   const int ii = min(i, d.im), jj = (j > d.jm) ? 1 : j;
-  if (N == 1) return {(r.a + r.b) / 2.f, dvs<P2, ZF>(-r.a + r.b, dx1[ii], d.gr.rdx1[ii], bd)};
+  if (N == 1) return {(r.a + r.b) / 2.f, dvs<P2, ZF>(-r.a + r.b, sx1<P2>(d, ii), rx1<P2>(d, ii), bd)};
   if (N == 2)
-    return {dvs<P2, ZF>(dx1[i + 1] * r.a + dx1[i] * r.b, dx1[i] + dx1[i + 1], d.gr.rdx1s[i], bd),
-            dvs<P2, ZF>(2.f * (-r.c + r.e), dy1[jj - 1] + dy1[jj], d.gr.rdy1s[jj - 1], bd)};
+    return {dvs<P2, ZF>(sx1<P2>(d, i + 1) * r.a + sx1<P2>(d, i) * r.b, sx1<P2>(d, i) + sx1<P2>(d, i + 1),
+                        rx1s<P2>(d, i), bd),
+            dvs<P2, ZF>(2.f * (-r.c + r.e), sy1<P2>(d, jj - 1) + sy1<P2>(d, jj), ry1s<P2>(d, jj - 1), bd)};
   if (N == 3) {
     if (k == 1)
-      return {dvs<P2, ZF>(0.5f * (dx1[i + 1] * r.a + dx1[i] * r.b), dx1[i] + dx1[i + 1], d.gr.rdx1s[i], bd), r.c};
-    return {dvs<P2, ZF>(dx1[i + 1] * r.a + dx1[i] * r.b, dx1[i] + dx1[i + 1], d.gr.rdx1s[i], bd),
+      return {dvs<P2, ZF>(0.5f * (sx1<P2>(d, i + 1) * r.a + sx1<P2>(d, i) * r.b), sx1<P2>(d, i) + sx1<P2>(d, i + 1),
+                          rx1s<P2>(d, i), bd),
+              r.c};
+    return {dvs<P2, ZF>(sx1<P2>(d, i + 1) * r.a + sx1<P2>(d, i) * r.b, sx1<P2>(d, i) + sx1<P2>(d, i + 1),
+                        rx1s<P2>(d, i), bd),
             dvz<ZF>(-r.c + r.e, d.gr.dzs[k - 1], d.gr.rdzs[k - 1], bd)};
   }
   if (N == 4)
-    return {dvs<P2, ZF>(dy1[j + 1] * r.a + dy1[j] * r.b, dy1[j] + dy1[j + 1], d.gr.rdy1s[j], bd) - 0.f,
-            dvs<P2, ZF>(2.f * (-r.c + r.e), dx1[ii - 1] + dx1[ii], d.gr.rdx1s[ii - 1], bd)};
-  if (N == 5) return {(r.a + r.b) / 2.f, dvs<P2, ZF>(-r.a + r.b, dy1[jj], d.gr.rdy1[jj], bd)};
+    return {dvs<P2, ZF>(sy1<P2>(d, j + 1) * r.a + sy1<P2>(d, j) * r.b, sy1<P2>(d, j) + sy1<P2>(d, j + 1),
+                        ry1s<P2>(d, j), bd) - 0.f,
+            dvs<P2, ZF>(2.f * (-r.c + r.e), sx1<P2>(d, ii - 1) + sx1<P2>(d, ii), rx1s<P2>(d, ii - 1), bd)};
+  if (N == 5) return {(r.a + r.b) / 2.f, dvs<P2, ZF>(-r.a + r.b, sy1<P2>(d, jj), ry1<P2>(d, jj), bd)};
   if (N == 6) {
     if (k == 1)
-      return {dvs<P2, ZF>(0.5f * (dy1[j + 1] * r.a + dy1[j] * r.b), dy1[j] + dy1[j + 1], d.gr.rdy1s[j], bd), r.c};
-    return {dvs<P2, ZF>(dy1[j + 1] * r.a + dy1[j] * r.b, dy1[j] + dy1[j + 1], d.gr.rdy1s[j], bd),
+      return {dvs<P2, ZF>(0.5f * (sy1<P2>(d, j + 1) * r.a + sy1<P2>(d, j) * r.b), sy1<P2>(d, j) + sy1<P2>(d, j + 1),
+                          ry1s<P2>(d, j), bd),
+              r.c};
+    return {dvs<P2, ZF>(sy1<P2>(d, j + 1) * r.a + sy1<P2>(d, j) * r.b, sy1<P2>(d, j) + sy1<P2>(d, j + 1),
+                        ry1s<P2>(d, j), bd),
             dvz<ZF>(-r.c + r.e, d.gr.dzs[k - 1], d.gr.rdzs[k - 1], bd)};
   }
   if (N == 7)
     return {dvz<ZF>(dzn[k + 1] * r.a + dzn[k] * r.b, dzn[k] + dzn[k + 1], d.gr.rdzsum[k], bd) - 0.f,
-            dvs<P2, ZF>(2.f * (-r.c + r.e), dx1[ii - 1] + dx1[ii], d.gr.rdx1s[ii - 1], bd)};
+            dvs<P2, ZF>(2.f * (-r.c + r.e), sx1<P2>(d, ii - 1) + sx1<P2>(d, ii), rx1s<P2>(d, ii - 1), bd)};
   if (N == 8)
     return {dvz<ZF>(dzn[k + 1] * r.a + dzn[k] * r.b, dzn[k] + dzn[k + 1], d.gr.rdzsum[k], bd),
-            dvs<P2, ZF>(2.f * (-r.c + r.e), dy1[jj - 1] + dy1[jj], d.gr.rdy1s[jj - 1], bd)};
+            dvs<P2, ZF>(2.f * (-r.c + r.e), sy1<P2>(d, jj - 1) + sy1<P2>(d, jj), ry1s<P2>(d, jj - 1), bd)};
   return {(r.a + r.b) / 2.f, dvz<ZF>(-r.a + r.b, dzn[k], d.gr.rdzn[k], bd)};  // N == 9
 }
 
@@ -171,14 +179,14 @@ template <bool P2, bool ZF>
 __device__ __forceinline__ float velfg_fu(const LesDom &d, int i, int j, int k, const NouDiu &a, const NouDiu &b,
                                           const NouDiu &y0, const NouDiu &y1, const NouDiu &z0, const NouDiu &z1,
                                           unsigned &bd) {
-  const float *dx1 = d.gr.dx1;
   const float covx1 =
-      dvs<P2, ZF>(dx1[i + 1] * (a.nou * a.diu) + dx1[i] * (b.nou * b.diu), dx1[i] + dx1[i + 1], d.gr.rdx1s[i], bd);
+      dvs<P2, ZF>(sx1<P2>(d, i + 1) * (a.nou * a.diu) + sx1<P2>(d, i) * (b.nou * b.diu),
+                  sx1<P2>(d, i) + sx1<P2>(d, i + 1), rx1s<P2>(d, i), bd);
   const float covy1 = (y0.nou * y0.diu + y1.nou * y1.diu) / 2.f;
   const float covz1 = (z0.nou * z0.diu + z1.nou * z1.diu) / 2.f;
   const float covc = covx1 + covy1 + covz1;
-  const float dfu1 = dvs<P2, ZF>(2.f * (-a.diu + b.diu), dx1[i] + dx1[i + 1], d.gr.rdx1s[i], bd) +
-                     dvs<P2, ZF>(-y0.diu + y1.diu, d.gr.dy1[j], d.gr.rdy1[j], bd) +
+  const float dfu1 = dvs<P2, ZF>(2.f * (-a.diu + b.diu), sx1<P2>(d, i) + sx1<P2>(d, i + 1), rx1s<P2>(d, i), bd) +
+                     dvs<P2, ZF>(-y0.diu + y1.diu, sy1<P2>(d, j), ry1<P2>(d, j), bd) +
                      dvz<ZF>(-z0.diu + z1.diu, d.gr.dzn[k], d.gr.rdzn[k], bd);
   return (-covc + d.vn * dfu1);
 }
@@ -186,14 +194,14 @@ template <bool P2, bool ZF>
 __device__ __forceinline__ float velfg_fv(const LesDom &d, int i, int j, int k, const NouDiu &a, const NouDiu &b,
                                           const NouDiu &y0, const NouDiu &y1, const NouDiu &z0, const NouDiu &z1,
                                           unsigned &bd) {
-  const float *dy1 = d.gr.dy1;
   const float covx1 = (a.nou * a.diu + b.nou * b.diu) / 2.f;
   const float covy1 =
-      dvs<P2, ZF>(dy1[j + 1] * (y0.nou * y0.diu) + dy1[j] * (y1.nou * y1.diu), dy1[j] + dy1[j + 1], d.gr.rdy1s[j], bd);
+      dvs<P2, ZF>(sy1<P2>(d, j + 1) * (y0.nou * y0.diu) + sy1<P2>(d, j) * (y1.nou * y1.diu),
+                  sy1<P2>(d, j) + sy1<P2>(d, j + 1), ry1s<P2>(d, j), bd);
   const float covz1 = (z0.nou * z0.diu + z1.nou * z1.diu) / 2.f;
   const float covc = covx1 + covy1 + covz1;
-  const float dfv1 = dvs<P2, ZF>(-a.diu + b.diu, d.gr.dx1[i], d.gr.rdx1[i], bd) +
-                     dvs<P2, ZF>(2.f * (-y0.diu + y1.diu), dy1[j] + dy1[j + 1], d.gr.rdy1s[j], bd) +
+  const float dfv1 = dvs<P2, ZF>(-a.diu + b.diu, sx1<P2>(d, i), rx1<P2>(d, i), bd) +
+                     dvs<P2, ZF>(2.f * (-y0.diu + y1.diu), sy1<P2>(d, j) + sy1<P2>(d, j + 1), ry1s<P2>(d, j), bd) +
                      dvz<ZF>(-z0.diu + z1.diu, d.gr.dzn[k], d.gr.rdzn[k], bd);
   return (-covc + d.vn * dfv1);
 }
@@ -207,8 +215,8 @@ __device__ __forceinline__ float velfg_fw(const LesDom &d, int i, int j, int k, 
   const float covz1 =
       dvz<ZF>(dzn[k + 1] * (z0.nou * z0.diu) + dzn[k] * (z1.nou * z1.diu), dzn[k] + dzn[k + 1], d.gr.rdzsum[k], bd);
   const float covc = covx1 + covy1 + covz1;
-  const float dfw1 = dvs<P2, ZF>(-a.diu + b.diu, d.gr.dx1[i], d.gr.rdx1[i], bd) +
-                     dvs<P2, ZF>(-y0.diu + y1.diu, d.gr.dy1[j], d.gr.rdy1[j], bd) +
+  const float dfw1 = dvs<P2, ZF>(-a.diu + b.diu, sx1<P2>(d, i), rx1<P2>(d, i), bd) +
+                     dvs<P2, ZF>(-y0.diu + y1.diu, sy1<P2>(d, j), ry1<P2>(d, j), bd) +
                      dvz<ZF>(-z0.diu + z1.diu, d.gr.dzs[k], d.gr.rdzs[k], bd);
   return (-covc + d.vn * dfw1);
 }
@@ -488,19 +496,23 @@ __global__ void __launch_bounds__(MTX *MTY) k_velfg_march_fix(LesDom d, uint3 g)
 // Smagorinsky face viscosity x/y interpolations: (dx1(i+1)*a + dx1(i)*b)/(dx1(i)+dx1(i+1))
 template <bool P2, bool ZF>
 __device__ __forceinline__ float ix_(const LesDom &d, int i, float a, float b, unsigned &bd) {
-  return dvs<P2, ZF>(d.gr.dx1[i + 1] * a + d.gr.dx1[i] * b, d.gr.dx1[i] + d.gr.dx1[i + 1], d.gr.rdx1s[i], bd);
+  return dvs<P2, ZF>(sx1<P2>(d, i + 1) * a + sx1<P2>(d, i) * b, sx1<P2>(d, i) + sx1<P2>(d, i + 1), rx1s<P2>(d, i),
+                     bd);
 }
 template <bool P2, bool ZF>  // (dx1(i)*a + dx1(i-1)*b)/(dx1(i-1)+dx1(i))
 __device__ __forceinline__ float ixm_(const LesDom &d, int i, float a, float b, unsigned &bd) {
-  return dvs<P2, ZF>(d.gr.dx1[i] * a + d.gr.dx1[i - 1] * b, d.gr.dx1[i - 1] + d.gr.dx1[i], d.gr.rdx1s[i - 1], bd);
+  return dvs<P2, ZF>(sx1<P2>(d, i) * a + sx1<P2>(d, i - 1) * b, sx1<P2>(d, i - 1) + sx1<P2>(d, i),
+                     rx1s<P2>(d, i - 1), bd);
 }
 template <bool P2, bool ZF>  // (dy1(j+1)*a + dy1(j)*b)/(dy1(j)+dy1(j+1))
 __device__ __forceinline__ float jy_(const LesDom &d, int j, float a, float b, unsigned &bd) {
-  return dvs<P2, ZF>(d.gr.dy1[j + 1] * a + d.gr.dy1[j] * b, d.gr.dy1[j] + d.gr.dy1[j + 1], d.gr.rdy1s[j], bd);
+  return dvs<P2, ZF>(sy1<P2>(d, j + 1) * a + sy1<P2>(d, j) * b, sy1<P2>(d, j) + sy1<P2>(d, j + 1), ry1s<P2>(d, j),
+                     bd);
 }
 template <bool P2, bool ZF>  // (dy1(j)*a + dy1(j-1)*b)/(dy1(j-1)+dy1(j))
 __device__ __forceinline__ float jym_(const LesDom &d, int j, float a, float b, unsigned &bd) {
-  return dvs<P2, ZF>(d.gr.dy1[j] * a + d.gr.dy1[j - 1] * b, d.gr.dy1[j - 1] + d.gr.dy1[j], d.gr.rdy1s[j - 1], bd);
+  return dvs<P2, ZF>(sy1<P2>(d, j) * a + sy1<P2>(d, j - 1) * b, sy1<P2>(d, j - 1) + sy1<P2>(d, j),
+                     ry1s<P2>(d, j - 1), bd);
 }
 
 // ---- diu as les reads the reference arrays, loaded from what velfg stored: the
@@ -603,15 +615,15 @@ struct ViscCol {
 struct ViscZ {
   float dznm, dznc, dznp, rdznc, rsumc, rsumm;
 };
+template <bool P2>
 __device__ __forceinline__ ViscCol visc_col(const LesDom &d, int i, int j) {
-  const LesGrid1 &g = d.gr;
   ViscCol c;
-  c.dx1m = g.dx1[i - 1]; c.dx1c = g.dx1[i]; c.dx1p = g.dx1[i + 1];
-  c.sxm = c.dx1m + c.dx1c; c.sxc = c.dx1c + c.dx1p; c.rsxm = g.rdx1s[i - 1]; c.rsxc = g.rdx1s[i];
-  c.dxs = g.dxs[i]; c.rdxs = g.rdxs[i]; c.rdx1 = g.rdx1[i];
-  c.dy1m = g.dy1[j - 1]; c.dy1c = g.dy1[j]; c.dy1p = g.dy1[j + 1];
-  c.sym = c.dy1m + c.dy1c; c.syc = c.dy1c + c.dy1p; c.rsym = g.rdy1s[j - 1]; c.rsyc = g.rdy1s[j];
-  c.dys = g.dys[j]; c.rdys = g.rdys[j]; c.rdy1 = g.rdy1[j];
+  c.dx1m = sx1<P2>(d, i - 1); c.dx1c = sx1<P2>(d, i); c.dx1p = sx1<P2>(d, i + 1);
+  c.sxm = c.dx1m + c.dx1c; c.sxc = c.dx1c + c.dx1p; c.rsxm = rx1s<P2>(d, i - 1); c.rsxc = rx1s<P2>(d, i);
+  c.dxs = sxs<P2>(d, i); c.rdxs = rxs<P2>(d, i); c.rdx1 = rx1<P2>(d, i);
+  c.dy1m = sy1<P2>(d, j - 1); c.dy1c = sy1<P2>(d, j); c.dy1p = sy1<P2>(d, j + 1);
+  c.sym = c.dy1m + c.dy1c; c.syc = c.dy1c + c.dy1p; c.rsym = ry1s<P2>(d, j - 1); c.rsyc = ry1s<P2>(d, j);
+  c.dys = sys<P2>(d, j); c.rdys = rys<P2>(d, j); c.rdy1 = ry1<P2>(d, j);
   return c;
 }
 __device__ __forceinline__ ViscZ visc_z(const LesDom &d, int k) {
@@ -730,7 +742,7 @@ __device__ __forceinline__ void visc_cell(const LesDom &d, int i, int j, int k, 
   v.f0 = d.f[c]; v.g0 = d.g[c]; v.h0 = d.h[c];
   v.ru = (k == 1) ? __ldg(&d.ruspd[(j + LES_JOFF) * d.pi + i + LES_IOFF]) : 0.f;
   v.rv = (k == 1) ? __ldg(&d.rvspd[(j + LES_JOFF) * d.pi + i + LES_IOFF]) : 0.f;
-  visc_compute<P2, ZF>(d, v, visc_col(d, i, j), visc_z(d, k), k, fv, gv, hv, bd);
+  visc_compute<P2, ZF>(d, v, visc_col<P2>(d, i, j), visc_z(d, k), k, fv, gv, hv, bd);
 }
 
 // adam.f95:30-44 (when AD; fo, go, ho: fold, gold, hold loaded by the caller ahead of
@@ -814,7 +826,7 @@ __global__ void __launch_bounds__(VTX *VTY, 2) k_les_visc_march(LesDom d) {
   put(S_E9 + (k0 & 1), 9, k0); put(S_E9 + ((k0 + 1) & 1), 9, k0 + 1);
   put(S_E7 + ((k0 - 1) & 1), 7, k0 - 1); put(S_E7 + (k0 & 1), 7, k0);
   put(S_E8 + ((k0 - 1) & 1), 8, k0 - 1); put(S_E8 + (k0 & 1), 8, k0);
-  const ViscCol cc = visc_col(d, ic, jc);
+  const ViscCol cc = visc_col<P2>(d, ic, jc);
   float ru = 0.f, rv = 0.f;
   if (k0 == 1) {
     ru = __ldg(&d.ruspd[(jc + LES_JOFF) * d.pi + ic + LES_IOFF]);

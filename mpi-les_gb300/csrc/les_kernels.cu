@@ -39,9 +39,9 @@ template <bool P2, bool ZF>
 __device__ __forceinline__ void velnw_cell(const LesDom &d, int i, int j, int k, int c, float &un, float &vn, float &wn,
                                            unsigned &bd) {
   const float pc = __ldg(d.p + c);
-  float pz = dvs<P2, ZF>(dvz<ZF>(-pc + __ldg(d.p + c + 1), d.ro, d.rro, bd), d.gr.dxs[i], d.gr.rdxs[i], bd);
+  float pz = dvs<P2, ZF>(dvz<ZF>(-pc + __ldg(d.p + c + 1), d.ro, d.rro, bd), sxs<P2>(d, i), rxs<P2>(d, i), bd);
   un = d.u[c] + d.dt * (__ldg(d.f + c) - pz);
-  pz = dvs<P2, ZF>(dvz<ZF>(-pc + __ldg(d.p + c + d.pi), d.ro, d.rro, bd), d.gr.dys[j], d.gr.rdys[j], bd);
+  pz = dvs<P2, ZF>(dvz<ZF>(-pc + __ldg(d.p + c + d.pi), d.ro, d.rro, bd), sys<P2>(d, j), rys<P2>(d, j), bd);
   vn = d.v[c] + d.dt * (__ldg(d.g + c) - pz);
   if (k <= d.km - 1) {
     pz = dvz<ZF>(dvz<ZF>(-pc + __ldg(d.p + c + d.np), d.ro, d.rro, bd), d.gr.dzs[k], d.gr.rdzs[k], bd);
@@ -264,11 +264,12 @@ __device__ __forceinline__ RhsIn rhs_load(const LesDom &d, int c) {
 }
 template <bool P2, bool ZF>
 __device__ __forceinline__ float rhs_comp(const LesDom &d, int i, int j, int k, const RhsIn &x, unsigned &bd) {
-  const float *dx1 = d.gr.dx1, *dy1 = d.gr.dy1, *dzn = d.gr.dzn;
-  const float rx = d.gr.rdx1[i], ry = d.gr.rdy1[j], rz = d.gr.rdzn[k];
-  const float r = dvs<P2, ZF>(-x.um + x.uc, dx1[i], rx, bd) + dvs<P2, ZF>(-x.vm + x.vc, dy1[j], ry, bd) +
+  const float *dzn = d.gr.dzn;
+  const float hx = sx1<P2>(d, i), hy = sy1<P2>(d, j);
+  const float rx = rx1<P2>(d, i), ry = ry1<P2>(d, j), rz = d.gr.rdzn[k];
+  const float r = dvs<P2, ZF>(-x.um + x.uc, hx, rx, bd) + dvs<P2, ZF>(-x.vm + x.vc, hy, ry, bd) +
                   dvz<ZF>(-x.wm + x.wc, dzn[k], rz, bd);
-  return dvs<P2, ZF>(x.fc - x.fm, dx1[i], rx, bd) + dvs<P2, ZF>(x.gc - x.gm, dy1[j], ry, bd) +
+  return dvs<P2, ZF>(x.fc - x.fm, hx, rx, bd) + dvs<P2, ZF>(x.gc - x.gm, hy, ry, bd) +
          dvz<ZF>(x.hc - x.hm, dzn[k], rz, bd) + dvz<ZF>(r, d.dt, d.rdt, bd);
 }
 template <bool P2, bool ZF>
