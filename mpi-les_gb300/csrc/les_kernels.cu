@@ -98,8 +98,8 @@ __global__ void __launch_bounds__(BX *BY) k_bondv1_fill(LesDom d) {
 }
 // uout = (max(0, max u(im)) + min(0, min u(im)))/2 (bondv1.f95:171-187).  The values
 // u(im, j, k) are one per row, so many blocks gather them; each block's max and min go
-// to part[], and the last block to finish combines them (max and min are exact in any
-// order).
+// to part[], and the last block to finish combines them, all its threads at once (max
+// and min are exact in any order).
 constexpr int UOUT_BLOCKS = 64, UOUT_THREADS = 256;
 __global__ void __launch_bounds__(UOUT_THREADS) k_bondv1_uout(LesDom d) {
   __shared__ float smax[UOUT_THREADS / 32], smin[UOUT_THREADS / 32];
@@ -127,13 +127,23 @@ __global__ void __launch_bounds__(UOUT_THREADS) k_bondv1_uout(LesDom d) {
     last = (atomicAdd(d.cnt + 12, 1u) == gridDim.x - 1);
   }
   __syncthreads();
-  if (!last || threadIdx.x != 0) return;
+  if (!last) return;
   __threadfence();
-  float a = 0.f, b = 0.f;
-  for (int q = 0; q < (int)gridDim.x; ++q) {
-    a = fmaxf(a, (float)((volatile double *)d.part)[2 * q]);
-    b = fminf(b, (float)((volatile double *)d.part)[2 * q + 1]);
+  aaa = 0.f;
+  bbb = 0.f;
+  for (int q = threadIdx.x; q < (int)gridDim.x; q += UOUT_THREADS) {
+    aaa = fmaxf(aaa, (float)((volatile double *)d.part)[2 * q]);
+    bbb = fminf(bbb, (float)((volatile double *)d.part)[2 * q + 1]);
   }
+  for (int o = 16; o > 0; o >>= 1) {
+    aaa = fmaxf(aaa, __shfl_down_sync(0xffffffffu, aaa, o));
+    bbb = fminf(bbb, __shfl_down_sync(0xffffffffu, bbb, o));
+  }
+  if ((threadIdx.x & 31) == 0) { smax[threadIdx.x >> 5] = aaa; smin[threadIdx.x >> 5] = bbb; }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  float a = 0.f, b = 0.f;
+  for (int q = 0; q < UOUT_THREADS / 32; ++q) { a = fmaxf(a, smax[q]); b = fminf(b, smin[q]); }
   const float uout = (a + b) / 2.f;
   d.fscal[SC_UOUT] = uout;
   d.scal[SC_UOUT] = (double)uout;
