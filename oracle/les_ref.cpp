@@ -111,6 +111,16 @@ struct Ref {
   FA<T> aveu, avev, avew, avep, avel, aveuu, avevv, aveww, avesm, avesmsm, uwfx;
   bool ave_alloc = false;
 
+  // trap_wall: stop with an error where the wall function would form 0/0 (a wall speed
+  // of zero, vel2.f95:138,173) instead of producing the NaN the reference produces
+  bool trap_wall = false;
+  void wall_check(T speed, int i, int j, const char *which) const {
+    if (!trap_wall || speed != L(0.)) return;
+    char b[160];
+    snprintf(b, sizeof b, "vel2.f95: %s(%d,%d) = 0: the wall function divides 0 by 0", which, i, j);
+    throw RefError{b};
+  }
+
   // diagnostics of the last step
   int last_iters = 0;
   double last_sor = 0, last_uout = 0, last_rhsav = 0, last_pav = 0, last_area = 0, last_pco = 0;
@@ -408,6 +418,7 @@ struct Ref {
     for (int j = 1; j <= jm; ++j)
       for (int i = 1; i <= im; ++i) {
         nou3(i, j, 1) = L(0.5) * (dx1(i + 1) * w(i, j, 1) + dx1(i) * w(i + 1, j, 1)) / (dx1(i) + dx1(i + 1));
+        wall_check(uspd(i, j), i, j, "uspd");
         diu3(i, j, 1) = uspd(i, j) * L(0.4) / std::log(L(0.5) * dzn(1) / L(0.1)) / (L(0.5) * dzn(1)) /
                         L(0.4) * u(i, j, 1) / uspd(i, j);
         cov3(i, j, 1) = nou3(i, j, 1) * diu3(i, j, 1);
@@ -434,6 +445,7 @@ struct Ref {
     for (int j = 1; j <= jm; ++j)
       for (int i = 1; i <= im; ++i) {
         nou6(i, j, 1) = L(0.5) * (dy1(j + 1) * w(i, j, 1) + dy1(j) * w(i, j + 1, 1)) / (dy1(j) + dy1(j + 1));
+        wall_check(vspd(i, j), i, j, "vspd");
         diu6(i, j, 1) = vspd(i, j) * L(0.4) / std::log(L(0.5) * dzn(1) / L(0.1)) / (L(0.5) * dzn(1)) /
                         L(0.4) * v(i, j, 1) / vspd(i, j);
         cov6(i, j, 1) = nou6(i, j, 1) * diu6(i, j, 1);
@@ -1249,6 +1261,14 @@ int ref_bounds_checked(void) {
 }
 
 const char *ref_last_error(void) { return g_err.c_str(); }
+
+int ref_trap_wall(void *hv, int on) {
+  Handle *h = (Handle *)hv;
+  if (!h) return -1;
+  if (h->f64) h->f64->trap_wall = on != 0;
+  else h->f32->trap_wall = on != 0;
+  return 0;
+}
 
 int ref_set_threads(int n) {
 #ifdef _OPENMP

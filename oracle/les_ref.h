@@ -70,6 +70,9 @@ const char *ref_last_error(void);
 /* threads of the fast build's parallel loops from now on (n > 0), for the calling
  * thread; returns the number its next loops will use (1 in the serial builds) */
 int ref_set_threads(int n);
+/* on != 0: a later velfg stops with an error (status -3, ref_last_error) where a wall
+ * speed is zero, the 0/0 of vel2.f95:138,173, instead of producing its NaN */
+int ref_trap_wall(void *h, int on);
 
 #ifdef __cplusplus
 }

@@ -57,6 +57,8 @@ def load(fast: bool = False) -> C.CDLL:
     lib.ref_last_error.restype = C.c_char_p
     lib.ref_set_threads.restype = C.c_int
     lib.ref_set_threads.argtypes = [C.c_int]
+    lib.ref_trap_wall.restype = C.c_int
+    lib.ref_trap_wall.argtypes = [vp, C.c_int]
     _libs[name] = lib
     return lib
 
@@ -104,6 +106,11 @@ class Ref:
 
     def step(self, n: int, nmax: int):
         self.stage(STEP, n, nmax)
+
+    def trap_wall(self, on: bool = True):
+        """Stop velfg with an error where a wall speed is zero (vel2.f95:138,173: the
+        reference forms 0/0 there) instead of carrying on with the NaN."""
+        self.lib.ref_trap_wall(self._h, 1 if on else 0)
 
     def aveflow(self, n: int, n1: int, nmax: int):
         """aveflow.f95: accumulate the time averages at step n (from n1), finalise at nmax."""

@@ -98,3 +98,29 @@ def test_fp32_stays_within_the_budget_of_fp64(oracle_built):
     lo, hi = (1, 1, 1), (sc.im, sc.jm, sc.km)
     for fid in (lesgpu.U, lesgpu.V, lesgpu.W, lesgpu.P):
         assert rel_err(a.get(fid, lo, hi), b.get(fid, lo, hi)) <= 1e-4, lesgpu.FIELD_NAMES[fid]
+
+
+def test_wall_at_rest_is_0_over_0(oracle_built):
+    """vel2.f95:138,173 divide by the wall speeds uspd, vspd: at rest on the first level
+    the reference forms 0/0.  The oracle's trap mode stops there and names the cell; by
+    default it carries the NaN on, as the reference does (the GPU parity test checks the
+    same NaN cells)."""
+    sc = scenario(32, 16, 8, seed=57)
+    st = random_state(sc, seed=157)
+    for fid in (lesgpu.U, lesgpu.V):
+        st[fid][8:15, 5:11, 1] = 0.0  # i 8..14, j 4..9 on k = 1
+    orc = make_ref(4, sc, lesgpu.Params(nmaxp=3))
+    for fid, a in st.items():
+        orc.set(fid, a.astype(np.float64))
+    orc.trap_wall(True)
+    with pytest.raises(RuntimeError, match="0 by 0"):
+        orc.stage(ref.VELFG)
+    orc.trap_wall(False)
+    for fid, a in st.items():
+        orc.set(fid, a.astype(np.float64))
+    orc.stage(ref.VELFG)
+    f = orc.get(lesgpu.F)  # (0:im, 0:jm, 0:km)
+    bad = np.argwhere(np.isnan(f[:, :, 1]))
+    assert bad.size, "no NaN where the wall speed is zero"
+    # every NaN of f at k = 1 lies next to the patch at rest (the faces of its cells)
+    assert bad[:, 0].min() >= 7 and bad[:, 0].max() <= 15 and bad[:, 1].min() >= 4 and bad[:, 1].max() <= 10, bad
