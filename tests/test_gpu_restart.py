@@ -161,3 +161,26 @@ def test_bad_files_fail_with_a_message(built_lib, tmp_path):
         gpu.read_restart(str(tmp_path / "junk"), p31)
     with pytest.raises(lesgpu.LesError, match="cannot open"):
         gpu.write_data20(str(tmp_path / "no" / "such" / "dir" / "data20"))
+
+
+def test_longer_records_are_read_like_fortran(built_lib, tmp_path):
+    """A Fortran read of fewer values than the record holds takes the first ones and
+    moves on to the next record (ifdata.f95:252-480 reads im*jm*km values per record):
+    records with trailing extra values, written by the independent writer, load the same
+    interiors as exact ones."""
+    import struct
+    sc = scenario(20, 12, 6, seed=67)
+    shape = (sc.im, sc.jm, sc.km)
+    rng = np.random.default_rng(68)
+    f30 = {nm: rng.standard_normal(shape).astype(np.float32) for nm in ftnio.DATA30}
+    f31 = {nm: rng.standard_normal(shape).astype(np.float32) for nm in ftnio.DATA31}
+    tail = np.arange(5, dtype=np.float32)
+    p30, p31 = str(tmp_path / "long30"), str(tmp_path / "long31")
+    ftnio.write_records(p30, [struct.pack(">if", 9, 0.4) + b"\0" * 8] +
+                        [np.concatenate([f30[nm].ravel(order="F"), tail]) for nm in ftnio.DATA30])
+    ftnio.write_records(p31, [np.concatenate([f31[nm].ravel(order="F"), tail]) for nm in ftnio.DATA31])
+    gpu = make_gpu(sc, lesgpu.Params())
+    n, t = gpu.read_restart(p30, p31)
+    assert (n, np.float32(t)) == (9, np.float32(0.4))
+    for nm, arr in {**f30, **f31}.items():
+        _same(gpu.download(IDS[nm], (1, 1, 1), shape), arr, nm)
