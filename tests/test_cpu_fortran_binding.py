@@ -48,3 +48,18 @@ def test_field_id_parameters_match_the_header():
         assert ids.get(m.group(1)) == int(m.group(2)), m.group(0)
         seen += 1
     assert seen >= 20
+
+
+def test_python_binding_arity_matches_the_header(built_lib):
+    """lesgpu's ctypes signatures take as many arguments as les_gpu.h declares."""
+    import lesgpu
+    lib = lesgpu.load_library()
+    c = _c_functions()
+    checked = 0
+    for name, nargs in c.items():
+        fn = getattr(lib, name, None)
+        if fn is None or fn.argtypes is None:
+            continue
+        assert len(fn.argtypes) == nargs, (name, len(fn.argtypes), nargs)
+        checked += 1
+    assert checked >= 40, checked
