@@ -341,7 +341,10 @@ enum les_prof {
   LES_PROF_VELFG = 1,  /* velfg (+ feedbf when fused in the step)                */
   LES_PROF_LES = 2,    /* les: eddy viscosity and viscous terms (+ adam fused)   */
   LES_PROF_VELNW = 3,
-  LES_PROF_STEP = 4    /* one whole step (n > 1)                                 */
+  LES_PROF_STEP = 4,   /* one whole step (n > 1)                                 */
+  LES_PROF_SOR_SWEEP = 5 /* the fused SOR sweep kernel alone: per launch, events
+                          * around sweeps 2..nmaxp of passes run as the step runs
+                          * them (the first sweep reads p, a different kernel)     */
 };
 int les_gpu_profile(les_handle *h, int what, int reps, double *ms_avg);
 

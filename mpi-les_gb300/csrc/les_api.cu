@@ -1040,6 +1040,29 @@ extern "C" int les_gpu_last_error(les_handle *h, char *buf, size_t len) {
 extern "C" int les_gpu_profile(les_handle *h, int what, int reps, double *ms_avg) {
   NEED_COMMIT(h);
   if (!ms_avg || reps < 1) return LES_ERR_ARG;
+  if (what == LES_PROF_SOR_SWEEP) {  // events around sweeps 2..nmaxp of each pass
+    std::vector<cudaEvent_t> ev(2 * (size_t)reps, nullptr);
+    for (auto &e : ev) CK(h, cudaEventCreate(&e));
+    LesCtx c = ctx_of(h);
+    int per = 0;
+    for (int r = 0; r < reps; ++r) per = les_step_sor_sweeps(h->dom, h->prm, &h->plan, c, ev[2 * r], ev[2 * r + 1]);
+    double total = 0.0;
+    int rc = LES_OK;
+    if (per > 0) {
+      CK(h, cudaEventSynchronize(ev.back()));
+      for (int r = 0; r < reps; ++r) {
+        float ms = 0.f;
+        CK(h, cudaEventElapsedTime(&ms, ev[2 * r], ev[2 * r + 1]));
+        total += ms;
+      }
+      *ms_avg = total / reps / per;
+    } else {
+      rc = fail(h, LES_ERR_STATE, "profile: this domain's SOR has no fused sweeps after the first");
+    }
+    CK(h, cudaStreamSynchronize(h->s));
+    for (auto &e : ev) cudaEventDestroy(e);
+    return rc ? rc : check_launch(h, "profile");
+  }
   cudaEvent_t a, b;
   CK(h, cudaEventCreate(&a));
   CK(h, cudaEventCreate(&b));

@@ -90,8 +90,9 @@ SorShape les_step_plan_shape(const LesDom &d, LesStepPlan *plan) {
 // the internal buffer X(l) (X = sorB for odd l, sorA for even l) or, for the last
 // iteration, p itself.  A copy-out moves the result into p when the sweep stopped
 // early (press.f95:119) or ran a single iteration.
+// ev_first / ev_last (optional) are recorded after the first and after the last sweep.
 static void enqueue_sor_fused(const LesDom &d, const les_params &prm, SorShape sh, const LesSorMaps *maps,
-                              LesCtx ctx) {
+                              LesCtx ctx, cudaEvent_t ev_first = nullptr, cudaEvent_t ev_last = nullptr) {
   les_launch_sor_begin(d, ctx);
   const int nit = prm.nmaxp;
   const int tiles = les_sor_fused_tiles(d.im, d.jm, sh);
@@ -112,6 +113,8 @@ static void enqueue_sor_fused(const LesDom &d, const les_params &prm, SorShape s
     a.counter = d.cnt;
     les_launch_sor_iter(d, a, sh, maps, ctx.s);
     ++*ctx.nlaunch;
+    if (l == 1 && ev_first) cudaEventRecord(ev_first, ctx.s);
+    if (l == nit && ev_last) cudaEventRecord(ev_last, ctx.s);
   }
   les_launch_sor_copyout(d, nit, ctx.s);
   ++*ctx.nlaunch;
@@ -171,6 +174,13 @@ int les_step_sor_pass(const LesDom &d, const les_params &prm, LesStepPlan *plan,
   ten.nmaxp = 10;
   enqueue_sor_fused(d, ten, plan->sor, &plan->maps, ctx);
   return 10;
+}
+int les_step_sor_sweeps(const LesDom &d, const les_params &prm, LesStepPlan *plan, LesCtx ctx, cudaEvent_t a,
+                        cudaEvent_t b) {
+  plan_pick(d, plan);
+  if (plan->sor.ny == 0 || prm.nmaxp < 2) return 0;
+  enqueue_sor_fused(d, prm, plan->sor, &plan->maps, ctx, a, b);  // the step's iteration count
+  return prm.nmaxp - 1;
 }
 void les_step_velfg_pass(const LesDom &d, LesCtx ctx) { les_launch_velfg_fused(d, true, ctx); }
 void les_step_les_pass(const LesDom &d, LesCtx ctx) { les_launch_les_fused(d, true, ctx); }

@@ -25,6 +25,10 @@ void les_step_plan_free(LesStepPlan *plan);
 int les_step_run(const LesDom &d, const les_params &prm, LesStepPlan *plan, int n, int nmax, LesCtx ctx);
 // Single passes of the step's heavy kernels, for profiling (les_gpu_profile).
 int les_step_sor_pass(const LesDom &d, const les_params &prm, LesStepPlan *plan, LesCtx ctx);  // iterations run
+// One SOR pass as the step runs it, with a recorded after the first sweep and b after the
+// last: returns the sweeps between them (0: no fused sweep for this domain)
+int les_step_sor_sweeps(const LesDom &d, const les_params &prm, LesStepPlan *plan, LesCtx ctx, cudaEvent_t a,
+                        cudaEvent_t b);
 SorShape les_step_pick_shape(const LesDom &d);
 // The plan's SOR shape (picked on first use): the automatic choice with the fixed
 // parts applied.

@@ -38,7 +38,7 @@ FIELD_NAMES = {
 }
 STATE_FIELDS = (U, V, W, P, F, G, H, FOLD, GOLD, HOLD, USUM, VSUM, WSUM)
 
-PROF_SOR, PROF_VELFG, PROF_LES, PROF_VELNW, PROF_STEP = range(5)
+PROF_SOR, PROF_VELFG, PROF_LES, PROF_VELNW, PROF_STEP, PROF_SOR_SWEEP = range(6)
 
 ERRORS = {0: "ok", -1: "bad argument", -2: "CUDA error", -3: "call out of order",
           -4: "out of device memory", -5: "non-finite values", -6: "busy", -7: "file error"}

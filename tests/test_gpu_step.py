@@ -242,3 +242,19 @@ def test_sor_early_exit_like_the_reference(built_lib, pjuge, lo, hi):
         assert e <= 1e-5, (nm, e)
         x, y = gpu.download(fid), stages.download(fid)
         assert np.array_equal(x.view(np.uint32), y.view(np.uint32)), nm
+
+
+def test_profile_modes(built_lib):
+    """les_gpu_profile: every stage times to a positive figure; the sweep-only SOR figure
+    times the fused sweeps after the first; a single-iteration SOR has none to time."""
+    sc = scenario(64, 40, 16, seed=71)
+    d = make_gpu(sc, lesgpu.Params(nmaxp=12))
+    d.step(1, 5)
+    for what in (lesgpu.PROF_SOR, lesgpu.PROF_VELFG, lesgpu.PROF_LES, lesgpu.PROF_VELNW, lesgpu.PROF_STEP,
+                 lesgpu.PROF_SOR_SWEEP):
+        ms = d.profile(what, 3)
+        assert 0.0 < ms < 1e3, (what, ms)
+    assert d.nonfinite() == 0
+    one = make_gpu(sc, lesgpu.Params(nmaxp=1))
+    with pytest.raises(lesgpu.LesError, match="no fused sweeps"):
+        one.profile(lesgpu.PROF_SOR_SWEEP, 2)
