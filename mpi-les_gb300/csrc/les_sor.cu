@@ -161,8 +161,9 @@ void les_launch_sor_iter(const LesDom &d, const SorArgs &a, SorShape sh, const L
     const char *e = getenv("LES_SOR_KIND");
     return e ? atoi(e) : 1;
   }();
+  // the TMA sweep is built for omega = 1 (press.f95:45); another omega takes the register kernel
   const bool tma = kind != 0 && maps && maps->valid && maps->shape.nx == sh.nx && maps->shape.ny == sh.ny &&
-                   cn1mode == 0 && (a.psrc == d.sorA || a.psrc == d.sorB);
+                   cn1mode == 0 && d.omega == 1.f && (a.psrc == d.sorA || a.psrc == d.sorB);
   const CUtensorMap *tp = tma ? ((a.psrc == d.sorA) ? &maps->m[0] : &maps->m[1]) : nullptr;
   const CUtensorMap *tr = tma ? &maps->m[2] : nullptr;
   if (sh.nx == 16) {

@@ -258,3 +258,24 @@ def test_profile_modes(built_lib):
     one = make_gpu(sc, lesgpu.Params(nmaxp=1))
     with pytest.raises(lesgpu.LesError, match="no fused sweeps"):
         one.profile(lesgpu.PROF_SOR_SWEEP, 2)
+
+
+@pytest.mark.parametrize("omega", [1.0, 1.3])
+def test_steps_with_relaxation_factor(built_lib, omega):
+    """omega of press.f95:45 (1 in the reference; the TMA sweep is built for it, any
+    other value runs the register sweep): the step graph equals the per-subroutine
+    sequence bit for bit, and both follow the FP32 oracle."""
+    sc = scenario(48, 32, 12, seed=73)
+    params = lesgpu.Params(omega=omega, nmaxp=15)
+    a = make_gpu(sc, params)
+    b = make_gpu(sc, params)
+    orc = make_ref(4, sc, params, sqrt_half=1, red64=1)
+    for n in range(1, 4):
+        a.step(n, 3)
+        b.velnw(); b.bondv1(n); b.velfg(); b.feedbf(); b.les(); b.adam(); b.press(n, 3)
+        orc.step(n, 3)
+    for fid, nm in FIELDS:
+        x, y = a.download(fid), b.download(fid)
+        assert np.array_equal(x.view(np.uint32), y.view(np.uint32)), nm
+        e = rel_err(_interior(a, fid, sc, True), _interior(orc, fid, sc, False))
+        assert e <= 1e-5, (nm, e)
