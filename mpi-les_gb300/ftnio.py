@@ -163,3 +163,67 @@ def data30_name(n: int) -> str:
 def data31_name(n: int) -> str:
     """anime.f95:492: '("data31",i6.6,".dat")'."""
     return f"data31{n:06d}.dat"
+
+
+LAYOUTS = {  # file kind -> (record names, leading (n, time) record)
+    "data20": (DATA20, False), "data21": (DATA21, False), "data30": (DATA30, True), "data31": (DATA31, False),
+    "data10": (DATA10, False), "data11": (DATA11, False),
+}
+
+
+def kind_of(path: str) -> str:
+    """The file kind from the reference's naming (data20, data30NNNNNN.dat, ...)."""
+    base = os.path.basename(path)
+    for k in LAYOUTS:
+        if base.startswith(k):
+            return k
+    raise ValueError(f"{path}: not one of the reference's file names ({', '.join(LAYOUTS)})")
+
+
+def compare(path_a: str, path_b: str, shape, kind: str | None = None) -> dict:
+    """Per-field differences of two files of one kind (a GPU run against a reference
+    run, two restarts, ...): {name: (max |a-b|, max |a-b| / max |b|)}, NaNs counted
+    as differences unless both sides hold them.  The files may differ in byte order."""
+    kind = kind or kind_of(path_a)
+    names, header = LAYOUTS[kind]
+    fa, na, ta = read_fields(path_a, names, shape, header=header)
+    fb, nb, tb = read_fields(path_b, names, shape, header=header)
+    out = {}
+    if header:
+        out["(n, time)"] = (float(abs(na - nb)), float(abs(np.float32(ta) - np.float32(tb))))
+    for nm in names:
+        a, b = fa[nm].astype(np.float64), fb[nm].astype(np.float64)
+        both_nan = np.isnan(a) & np.isnan(b)
+        d = np.where(both_nan, 0.0, np.abs(a - b))
+        d = np.where(np.isnan(d), np.inf, d)
+        scale = float(np.nanmax(np.abs(b))) if np.isfinite(b).any() else 0.0
+        dmax = float(d.max()) if d.size else 0.0
+        out[nm] = (dmax, dmax / scale if scale > 0 else (0.0 if dmax == 0 else np.inf))
+    return out
+
+
+def main(argv=None) -> int:
+    """python ftnio.py FILE [FILE2] --dims IMxJMxKM: list the records of a reference file
+    (per field min, max, mean) or compare two (per field max abs and relative difference)."""
+    import argparse
+    ap = argparse.ArgumentParser(description=main.__doc__)
+    ap.add_argument("files", nargs="+")
+    ap.add_argument("--dims", required=True, help="IMxJMxKM of the domain the file holds")
+    args = ap.parse_args(argv)
+    shape = tuple(int(x) for x in args.dims.split("x"))
+    if len(args.files) == 2:
+        for nm, (dabs, drel) in compare(args.files[0], args.files[1], shape).items():
+            print(f"{nm:10s} max |a-b| {dabs:.6g}   relative {drel:.3g}")
+        return 0
+    path = args.files[0]
+    names, header = LAYOUTS[kind_of(path)]
+    fields, n, t = read_fields(path, names, shape, header=header)
+    print(f"{path}: {'big' if detect_order(path) else 'little'}-endian" + (f", n = {n}, time = {t:g}" if header else ""))
+    for nm in names:
+        a = fields[nm]
+        print(f"{nm:10s} min {np.nanmin(a):.6g}  max {np.nanmax(a):.6g}  mean {np.nanmean(a):.6g}")
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())

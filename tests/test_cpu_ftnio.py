@@ -111,3 +111,24 @@ def test_bad_markers_are_refused(tmp_path):
     p.write_bytes(_be(8) + b"1234")
     with pytest.raises(ValueError):
         ftnio.detect_order(str(p))
+
+
+def test_compare_two_runs_files(tmp_path):
+    """ftnio.compare: per-field differences of two files of one kind, in either byte
+    order (a GPU run's data20 against a reference run's)."""
+    rng = np.random.default_rng(8)
+    shape = (6, 5, 4)
+    a = {nm: rng.standard_normal(shape).astype(np.float32) for nm in ftnio.DATA20}
+    b = {nm: v.copy() for nm, v in a.items()}
+    b["p"][2, 3, 1] += np.float32(0.5)
+    b["w"][0, 0, 0] = np.nan
+    pa, pb = tmp_path / "data20", tmp_path / "data20.le"
+    ftnio.write_fields(str(pa), a, ftnio.DATA20)
+    ftnio.write_fields(str(pb), b, ftnio.DATA20, big_endian=False)
+    d = ftnio.compare(str(pa), str(pb), shape, kind="data20")
+    assert d["u"] == (0.0, 0.0)
+    assert abs(d["p"][0] - 0.5) < 1e-6 and d["p"][1] > 0
+    assert d["w"][0] == np.inf
+    assert ftnio.kind_of(str(tmp_path / ftnio.data30_name(5))) == "data30"
+    assert ftnio.main([str(pa), "--dims", "6x5x4"]) == 0
+    assert ftnio.main([str(pa), str(pb), "--dims", "6x5x4"]) == 0
