@@ -239,11 +239,14 @@ contains
 
   ! Upload the state, grid, coefficients, masks and the inflow profile of
   ! bondv1.f95:33-54 (5 m/s up to k = 78, u(77) above, v = w = 0), then commit.
-  ! Replaces initialise_LES_kernel (main.f95:229-233).
+  ! Replaces initialise_LES_kernel (main.f95:229-233).  press leaves its SOR loop
+  ! once sor < pjuge (press.f95:119-121), as the reference does; the optional
+  ! fixed_sor = .true. always runs nmaxp = 50 iterations instead (throughput runs).
   subroutine initialise_LES_gpu(p, u, v, w, usum, vsum, wsum, f, g, h, fold, gold, hold, &
                                 bmask1, cmask1, dmask1, cn1, cn2l, cn2s, cn3l, cn3s, cn4l, cn4s, &
-                                dxs, dys, dzs, dx1, dy1, dzn, z2, dt, im, jm, km)
+                                dxs, dys, dzs, dx1, dy1, dzn, z2, dt, im, jm, km, fixed_sor)
     integer, intent(in) :: im, jm, km
+    logical, intent(in), optional :: fixed_sor
     real(4), intent(in) :: dt
     real(4), intent(in) :: p(0:im+2, 0:jm+2, 0:km+1)
     real(4), intent(in) :: u(0:im+1, -1:jm+1, 0:km+1), v(0:im+1, -1:jm+1, 0:km+1)
@@ -260,9 +263,15 @@ contains
     type(les_params) :: prm
     real(4), allocatable :: inflow(:, :), zero(:, :)
     integer :: k
+    integer(c_int) :: sor_fixed
+    sor_fixed = 0
+    if (present(fixed_sor)) then
+      if (fixed_sor) sor_fixed = 1
+    end if
     dims = les_dims(im, jm, km)
-    ! set.f95:89-95 and press.f95:43-45
-    prm = les_params(dt, 1.1763, 15.83e-6, -10.0, -1.0, 1.0, 1.0e-4, 50, 1, 0)
+    ! set.f95:89-95 (dt, ro, vn, alpha, beta) and press.f95:43-45 (omega, pjuge,
+    ! nmaxp); sor_fixed = 0 is press.f95:119-121's exit on sor < pjuge
+    prm = les_params(dt, 1.1763, 15.83 * 10.**(-6.), -10., -1., 1., 0.0001, 50, sor_fixed, 0)
     call check(les_gpu_create(dims, prm, les_h), 'create')
     call put3(LES_FIELD_P, p, 0, im + 2, 0, jm + 2, 0, km + 1)
     call put3(LES_FIELD_U, u, 0, im + 1, -1, jm + 1, 0, km + 1)
