@@ -230,9 +230,10 @@ int les_gpu_stream(les_handle *h, void **stream);
  * shared by all calls, which keeps what the last call left (each call clears what must
  * start at zero).  Calls that overlap in time race on it.  The array's address is
  * looked up on the first call from a device: make that call outside stream capture.
- * Domains with more than LES_NOALLOC_MAX_PARTS interior blocks ((im+63)/64 *
- * (jm+3)/4 * km) are refused with LES_ERR_ARG.  Synchronises the handle's stream. */
-#define LES_NOALLOC_MAX_PARTS 262144 /* 2 MiB of FP64 block partials */
+ * Domains with more than LES_NOALLOC_MAX_PARTS reduction blocks of 64 x 4 x 16 cells
+ * ((im+63)/64 * (jm+3)/4 * ((km+15)/16); 600x600x90 has 9000) are refused with
+ * LES_ERR_ARG.  Synchronises the handle's stream. */
+#define LES_NOALLOC_MAX_PARTS 65536 /* 512 KiB of FP64 block partials */
 int les_gpu_field_mean_noalloc(les_handle *h, int field, double *mean);
 /* Kernel launches issued on this handle since creation (all stages). */
 long long les_gpu_launch_count(les_handle *h);

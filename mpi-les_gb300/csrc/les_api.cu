@@ -795,10 +795,10 @@ extern "C" int les_gpu_field_mean_noalloc(les_handle *h, int field, double *mean
     return fail(h, LES_ERR_ARG, "field_mean_noalloc: field must be a 3-D field (LES_FIELD_U .. LES_FIELD_SM)");
   LesDom shape{};
   shape.im = h->dims.im; shape.jm = h->dims.jm; shape.km = h->dims.km;
-  const long long nparts = les_interior_blocks(shape);
+  const long long nparts = les_reduce_blocks(shape);
   if (nparts > LES_NOALLOC_MAX_PARTS)
     return fail(h, LES_ERR_ARG, "field_mean_noalloc: the domain has " + std::to_string(nparts) +
-                                    " interior blocks ((im+63)/64*(jm+3)/4*km); the static scratch holds " +
+                                    " reduction blocks ((im+63)/64*(jm+3)/4*((km+15)/16)); the static scratch holds " +
                                     std::to_string(LES_NOALLOC_MAX_PARTS));
   NEED_COMMIT(h);
   std::string err;

@@ -645,6 +645,11 @@ int les_interior_blocks(const LesDom &d) {
   return (int)(g.x * g.y * g.z);
 }
 
+int les_reduce_blocks(const LesDom &d) {
+  const dim3 g = reduce_grid(d);
+  return (int)(g.x * g.y * g.z);
+}
+
 void les_launch_rhs_mean(const LesDom &d, LesCtx ctx) {
   launch_rhs(d, d.rhs, 0, ctx);
   LAUNCH(ctx, k_sub_mean<<<sub_mean_blocks(d), 32 * SUB_ROWS, 0, ctx.s>>>(d, d.rhs, SC_RHSAV));

@@ -33,7 +33,7 @@ void les_launch_sor_begin(const LesDom &d, LesCtx ctx);
 // Blocks of the second reduction level of k_finish_mean (buffer d.part2).
 constexpr int LES_FIN_BLOCKS = 128;
 // The volume-weighted interior mean of d.p (press.f95:124-133, the pav reduction) into
-// d.fscal[SC_PAV] and d.scal[SC_PAV]; partials in d.part (les_interior_blocks(d)
+// d.fscal[SC_PAV] and d.scal[SC_PAV]; partials in d.part (les_reduce_blocks(d)
 // doubles), d.part2 (LES_FIN_BLOCKS doubles), ticket d.cnt[8] (zero on entry, zero on
 // exit); reads d.scal[SC_AREA].
 void les_launch_interior_mean(const LesDom &d, LesCtx ctx);
@@ -41,4 +41,6 @@ void les_launch_sor_simple(const LesDom &d, int nmaxp, LesCtx ctx);
 void les_launch_pav_adjust(const LesDom &d, LesCtx ctx);
 void les_launch_count_nonfinite(const LesDom &d, unsigned long long *bad, LesCtx ctx);
 int les_interior_blocks(const LesDom &d);
+// Blocks (= partial sums) of the rhs and pav reductions: (im+63)/64 * (jm+3)/4 * ((km+15)/16)
+int les_reduce_blocks(const LesDom &d);
 int les_sor_simple_parts(const LesDom &d);

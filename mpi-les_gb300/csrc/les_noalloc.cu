@@ -11,9 +11,9 @@
 // sums of x*dx1*dy1*dzn, a fixed-order two-level FP64 finish, divided by the FP64
 // domain volume, rounded to FP32 as press rounds pav.
 //
-// Limits and sharing.  The scratch holds LES_NOALLOC_MAX_PARTS block partials: a
-// domain with more interior blocks ((im+63)/64 * (jm+3)/4 * km) is refused with
-// LES_ERR_ARG.  All calls in the process share the one array per device and it keeps
+// Limits and sharing.  The scratch holds LES_NOALLOC_MAX_PARTS block partials, one
+// per 64 x 4 x 16 cells: a domain with more reduction blocks ((im+63)/64 * (jm+3)/4 *
+// ((km+15)/16), les_reduce_blocks) is refused with LES_ERR_ARG.  All calls in the process share the one array per device and it keeps
 // what the last call left there; each call clears the words that must start at zero
 // (the completion ticket).  Two calls whose kernels overlap in time (different
 // streams or threads without ordering) race on the array and give wrong results.
@@ -74,9 +74,9 @@ int scratch_on(int dev, double **out, std::string *err) {
 
 int les_noalloc_interior_mean(const LesDom &dom, const float *x, const double *area_dev, cudaStream_t s,
                               long long *nlaunch, int dev, double *mean, std::string *err) {
-  if (les_interior_blocks(dom) > kParts) {
-    *err = "field_mean_noalloc: the domain has " + std::to_string(les_interior_blocks(dom)) +
-           " interior blocks; the static scratch holds " + std::to_string(kParts);
+  if (les_reduce_blocks(dom) > kParts) {
+    *err = "field_mean_noalloc: the domain has " + std::to_string(les_reduce_blocks(dom)) +
+           " reduction blocks; the static scratch holds " + std::to_string(kParts);
     return LES_ERR_ARG;
   }
   double *sc = nullptr;
