@@ -2,16 +2,18 @@
 
 The reference ships no golden vectors for the solver, so the oracle's restatement is
 held to it by its loop-by-loop citations and by answers the equations fix exactly:
-a uniform pressure with no forcing leaves velnw's velocities unchanged, adam maps a
-constant history to itself, feedbf does nothing where the building masks are zero,
-press removes the volume-weighted mean of p, the oracle is deterministic, and FP32
-drifts from FP64 within the 1e-4 budget of the parity contract.
+a uniform pressure with no forcing leaves velnw's velocities unchanged, a uniform
+flow gives velfg no advection and only the wall function's diffusion at the first
+level, adam maps a constant history to itself, feedbf does nothing where the building
+masks are zero, press's SOR converges to a manufactured pressure, press removes the
+volume-weighted mean of p, the oracle is deterministic, and FP32 drifts from FP64
+within the 1e-4 budget of the parity contract.
 """
 import numpy as np
 import pytest
 
 import lesgpu
-from helpers import STATE, make_ref, random_state, rel_err, scenario
+from helpers import STATE, make_ref, manufactured_pressure, random_state, rel_err, scenario
 from oracle import ref
 
 
@@ -38,6 +40,66 @@ def test_velnw_uniform_pressure_no_forcing_keeps_velocities(oracle_built):
     orc.stage(ref.VELNW)
     for fid in (lesgpu.U, lesgpu.V, lesgpu.W):
         assert np.array_equal(orc.get(fid).astype(np.float32), st[fid]), lesgpu.FIELD_NAMES[fid]
+
+
+def uniform_flow(sc, U):
+    """u = U, v = w = 0 over the full declared extents (halos too)."""
+    out = {}
+    for fid in (lesgpu.U, lesgpu.V, lesgpu.W):
+        lb, ub = lesgpu.declared_extents(fid, sc.im, sc.jm, sc.km)
+        out[fid] = np.full(tuple(ub[q] - lb[q] + 1 for q in range(3)), U if fid == lesgpu.U else 0.0,
+                           np.float32, order="F")
+    return out
+
+
+def velfg_uniform_expectation(f, g, h, km, U, vn, dzn1, tol):
+    """velFG.f95:64-110 for u = U, v = w = 0: every advective flux cov1..9 and every
+    gradient diu1..9 vanishes except the log-law wall gradient diu3(i,j,1) = U /
+    (alog(0.5 dzn(1)/0.1) * 0.5 dzn(1)) of vel2.f95:138, so g = 0, h = 0 (k < km),
+    f = 0 for k >= 2, and f(i,j,1) = vn * (-diu3(1) + 0) / dzn(1)."""
+    # f, g, h over (0:im, 0:jm, 0:km): interior [1:, 1:, 1:]
+    assert np.all(g[1:, 1:, 1:] == 0.0)
+    assert np.all(h[1:, 1:, 1:km] == 0.0)
+    assert np.all(f[1:, 1:, 2:] == 0.0)
+    hz = 0.5 * dzn1
+    f1 = -vn * (U / (np.log(hz / 0.1) * hz)) / dzn1
+    got = f[1:, 1:, 1]
+    assert np.all(np.abs(got - f1) <= tol * abs(f1)), (got.min(), got.max(), f1)
+
+
+@pytest.mark.parametrize("prec", [4, 8])
+def test_velfg_uniform_flow_has_no_advection(oracle_built, prec):
+    sc = scenario(24, 14, 10, seed=3, coverage=0.0)
+    params = lesgpu.Params()
+    orc = make_ref(prec, sc, params)
+    U = 3.0
+    for fid, a in uniform_flow(sc, U).items():
+        orc.set(fid, a.astype(np.float64))
+    orc.stage(ref.VELFG)
+    dzn1 = float(orc.get(lesgpu.DZN).ravel()[2])
+    vn = float(np.float32(params.vn)) if prec == 4 else 15.83e-6
+    velfg_uniform_expectation(orc.get(lesgpu.F), orc.get(lesgpu.G), orc.get(lesgpu.H), sc.km, U, vn, dzn1,
+                              4e-7 if prec == 4 else 1e-13)
+
+
+@pytest.mark.parametrize("prec,tol", [(8, 2e-7), (4, 3e-5)])
+def test_press_sor_converges_to_a_manufactured_pressure(oracle_built, prec, tol):
+    """press.f95:47-159 on rhs = A p* (A the SOR's own operator, press.f95:93-96):
+    3000 fixed iterations from p = 0 reach p* minus its volume-weighted mean."""
+    im, jm, km = 32, 16, 12
+    sc = scenario(im, jm, km, seed=3, coverage=0.0)
+    n = 3000
+    o64 = make_ref(8, sc, lesgpu.Params(nmaxp=n, sor_fixed=1))
+    u, expect = manufactured_pressure(o64, im, jm, km)
+    orc = o64 if prec == 8 else make_ref(4, sc, lesgpu.Params(nmaxp=n, sor_fixed=1))
+    for fid in (lesgpu.V, lesgpu.W, lesgpu.F, lesgpu.G, lesgpu.H, lesgpu.P):
+        lb, ub = orc.extents(fid)
+        orc.set(fid, np.zeros(tuple(ub[q] - lb[q] + 1 for q in range(3))))
+    orc.set(lesgpu.U, u.astype(np.float32).astype(np.float64) if prec == 4 else u)
+    orc.stage(ref.PRESS, 2, 10)
+    assert orc.diag()["iters"] == n
+    p = orc.get(lesgpu.P, (1, 1, 1), (im, jm, km))
+    assert rel_err(p, expect) <= tol, rel_err(p, expect)
 
 
 def test_adam_keeps_a_constant_history(oracle_built):
