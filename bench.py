@@ -26,7 +26,8 @@ exchange), so per-GPU work is fixed as N grows ("scaling": "weak").
 
 --impl reference times the CPU restatement of the reference's les_main (the oracle:
 the Fortran reference cannot be compiled on this image, there is no Fortran
-compiler) on the host cores, on a bounded sample of the same workload.
+compiler) on the host cores, on the same 600x600x90 workload, with inputs from the
+oracle's own scenario generator (the GPU library is not loaded).
 """
 from __future__ import annotations
 
@@ -162,62 +163,85 @@ def reduce_max(pg, x: float) -> float:
     return float(t.item())
 
 
-def cpu_baseline_sample(threads: int | None = None, im=150, jm=150, km=90, steps=25):
-    """Time the oracle (CPU restatement of les_main's solver) on a bounded sample."""
-    import lesgpu
+def oracle_domain(im=IM, jm=JM, km=KM, seed=1, prec=4, threads=None):
+    """The workload's domain in the oracle's fast build (gfortran semantics: x**0.5 as
+    powf, FP32 sums), its inputs made by the oracle's own scenario generator -- nothing
+    of the GPU product is loaded.  Returns (Ref, threads in use)."""
     from oracle import ref as oref
-    sc = scenario(seed=1, im=im, jm=jm, km=km)
-    zbm, uin, vin, win = lesgpu.generate_scenario(sc)
+    zbm, uin, vin, win = oref.scenario(im, jm, km, seed, fast=True)
     used = oref.set_threads(threads or (os.cpu_count() or 1))
-    r = oref.Ref(4, im, jm, km, zbm, uin, vin, win, sqrt_half=0, red64=0, fast=True)
-    r.step(1, steps + 1)  # warm-up (n == 1 fill)
-    # the step's seven subroutines in main.f95's order, each timed (oracle's step() is
-    # exactly this sequence)
-    order = (("velnw", oref.VELNW), ("bondv1", oref.BONDV1), ("velfg", oref.VELFG), ("feedbf", oref.FEEDBF),
-             ("les", oref.LES), ("adam", oref.ADAM), ("press", oref.PRESS))
-    per = {nm: 0.0 for nm, _ in order}
+    r = oref.Ref(prec, im, jm, km, zbm, uin, vin, win, sqrt_half=0, red64=0, fast=True)
+    return r, used
+
+
+STAGE_ORDER = ("velnw", "bondv1", "velfg", "feedbf", "les", "adam", "press")
+
+
+def timed_oracle_steps(r, n0, steps, nmax):
+    """Steps n0 .. n0+steps-1 of the oracle, each of the seven subroutines of main.f95's
+    order timed (the oracle's step() is exactly this sequence).  Returns (seconds,
+    seconds per step of each subroutine)."""
+    from oracle import ref as oref
+    ids = dict(zip(STAGE_ORDER, (oref.VELNW, oref.BONDV1, oref.VELFG, oref.FEEDBF, oref.LES, oref.ADAM, oref.PRESS)))
+    per = {nm: 0.0 for nm in STAGE_ORDER}
     t0 = time.perf_counter()
-    for n in range(2, steps + 2):
-        for nm, st in order:
+    for n in range(n0, n0 + steps):
+        for nm in STAGE_ORDER:
             ts = time.perf_counter()
-            r.stage(st, n, steps + 1)
+            r.stage(ids[nm], n, nmax)
             per[nm] += time.perf_counter() - ts
     dt = time.perf_counter() - t0
+    return dt, {nm: round(v / steps, 6) for nm, v in per.items()}
+
+
+def cpu_baseline_sample(threads: int | None = None, im=150, jm=150, km=90, steps=25):
+    """Time the oracle (CPU restatement of les_main's solver) on a bounded sample."""
+    r, used = oracle_domain(im, jm, km, threads=threads)
+    r.step(1, steps + 1)  # warm-up (n == 1 fill)
+    dt, per_step = timed_oracle_steps(r, 2, steps, steps + 1)
     r.close()
-    per_step = {nm: round(v / steps, 6) for nm, v in per.items()}
     return (im * jm * km * steps / dt, f"{steps} steps of {im}x{jm}x{km} after 1 warm-up step, {dt:.1f} s", used,
             per_step)
 
 
 def run_reference(args):
-    world, rank, local, pg = dist_setup()
-    if rank != 0:
+    """The reference's CPU path on this host: the oracle's fast build (the Fortran
+    reference cannot be compiled here: no Fortran compiler) on the workload's own
+    600x600x90 domain, all host threads (OpenMP over k planes, the role les_main_mpi's
+    decomposition plays), then the same domain on one thread (les_main's role) for a few
+    steps beside it.  Under torchrun only rank 0 runs; the other ranks exit at once."""
+    if int(os.environ.get("RANK", "0")) != 0:
         return 0
     from oracle import ref as oref
     oref.build()
-    import lesgpu
-    threads = oref.set_threads(os.cpu_count() or 1)
-    # one "step" = one oracle time step on a 300x300x90 sample of the workload's domain
-    im, jm, km = 300, 300, 90
-    sc = scenario(seed=1, im=im, jm=jm, km=km)
-    zbm, uin, vin, win = lesgpu.generate_scenario(sc)
-    r = oref.Ref(4, im, jm, km, zbm, uin, vin, win, sqrt_half=0, red64=0, fast=True)
+    im, jm, km = args.dims  # the workload's 600x600x90 unless --dims says otherwise
+    cells = im * jm * km
+    nmax = args.warmup + args.steps + 10**6
+    r, threads = oracle_domain(im, jm, km)
     n = 1
     for _ in range(args.warmup):
-        r.step(n, 10**6)
+        r.step(n, nmax)
         n += 1
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        r.step(n, 10**6)
-        n += 1
-    dt = time.perf_counter() - t0
-    val = im * jm * km * args.steps / dt
+    dt, per_step = timed_oracle_steps(r, n, args.steps, nmax)
+    n += args.steps
+    val = cells * args.steps / dt
+    # one thread, the same domain and state, a few steps
+    one_steps = 2
+    used1 = oref.set_threads(1)
+    dt1, per1 = timed_oracle_steps(r, n, one_steps, nmax)
+    r.close()
     line = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "config": workload_config(),
+            "data": "synthetic: seeded urban heightmap and power-law inflow (the oracle's own generator)",
+            "config": workload_config(im, jm, km),
             "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"each step: one oracle time step on a {im}x{jm}x{km} sample of the domain"},
+                             "sample": f"each step: one full time step of the {im}x{jm}x{km} domain "
+                                       f"(the configuration named in config), {threads} threads",
+                             "stage_s_per_step": per_step},
+            "single_core": {"value": cells * one_steps / dt1, "unit": UNIT, "cores": used1,
+                            "sample": f"{one_steps} further steps of the same {im}x{jm}x{km} domain on one thread "
+                                      "(les_main's role)", "stage_s_per_step": per1},
             "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0

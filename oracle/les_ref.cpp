@@ -1270,6 +1270,103 @@ int ref_trap_wall(void *hv, int on) {
   return 0;
 }
 
+/* The configs' seeded synthetic scenario, restated here so that the checker and the
+ * timed CPU baseline need nothing from the product.  Inputs: fl[] = {dz0, dz_ratio,
+ * coverage, h_min, h_max, u_ref, z_ref, pl_exp, direction_deg, noise} (FP32 values, as
+ * the product's les_scenario holds them), in[] = {dz_law, fp_min, fp_max, inflow_law}.
+ * Heightmap: rectangular blocks, footprint sides uniform in [fp_min, fp_max] cells,
+ * heights uniform in [h_min, h_max] m, drawn with SplitMix64 (Steele, Lea, Flood,
+ * OOPSLA 2014) until the plan coverage is met, i within [max(3,im/8), im-max(3,im/8)],
+ * j periodic.  Inflow planes (1:jm,1:km): U(z) = u_ref (z/z_ref)^pl_exp at z =
+ * z2(k) + 0.5 dzn(k) (bondv1.f95:36's height; inflow_law 0: the reference's 5 m/s),
+ * turned by the residual of the direction after whole quarter turns, r in [-45, 45)
+ * degrees: (u, v) = U (cos r, sin r), plus a fixed uniform +-noise per cell and
+ * component.  z2 and dzn are the FP32 grid of grid.f95:114-135 (dz_law 0) or the
+ * geometric law (dz_law 1), as ref_create builds them. */
+int ref_scenario(int im, int jm, int km, const float *fl, const int *in, unsigned long long seed, float *zbm,
+                 float *uin, float *vin, float *win) {
+  if (im < 3 || jm < 2 || km < 3 || !fl || !in || !zbm || !uin || !vin || !win) {
+    g_err = "ref_scenario: bad arguments";
+    return -1;
+  }
+  const float dz0 = fl[0], dzr = fl[1], coverage = fl[2], h_min = fl[3], h_max = fl[4], u_ref = fl[5];
+  const float z_ref = fl[6], pl_exp = fl[7], direction = fl[8], noise = fl[9];
+  const int dz_law = in[0], fp_min = in[1], fp_max = in[2], inflow_law = in[3];
+  // vertical grid in FP32 (the same loops as Ref<float>::grid)
+  std::vector<float> dzn(km + 4, 0.f), z2(km + 3, 0.f);  // dzn(k) at [k+1], z2(k) at [k]
+  if (dz_law == 0) {
+    if (km < 58) { g_err = "ref_scenario: the reference dz law needs km >= 58"; return -1; }
+    z2[0] = 1.f; dzn[1] = 1.f; z2[1] = 1.f; dzn[2] = 1.f;
+    for (int k = 2; k <= 15; ++k) dzn[k + 1] = dzn[k] * 1.1f;
+    for (int k = 16; k <= 44; ++k) dzn[k + 1] = 4.f;
+    for (int k = 45; k <= 58; ++k) dzn[k + 1] = dzn[k] * 1.1f;
+    for (int k = 59; k <= km + 1; ++k) dzn[k + 1] = 16.f;
+  } else {
+    z2[0] = dz0; dzn[1] = dz0; z2[1] = dz0; dzn[2] = dz0;
+    for (int k = 2; k <= km + 1; ++k) dzn[k + 1] = dzn[k] * dzr;
+  }
+  for (int k = 2; k <= km + 2; ++k) z2[k] = z2[k - 1] + dzn[k + 1];
+  dzn[km + 2] = dzn[km + 1];
+  // SplitMix64 stream
+  uint64_t st = (uint64_t)seed ^ 0x4c45535f47423330ull;
+  auto next = [&]() {
+    uint64_t z = (st += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+  };
+  auto uni = [&]() { return (double)(next() >> 11) * (1.0 / 9007199254740992.0); };
+  auto irange = [&](int a, int b) { return a + (int)(uni() * (double)(b - a + 1)); };
+  for (size_t q = 0; q < (size_t)im * jm; ++q) zbm[q] = 0.f;
+  if (coverage > 0.f) {
+    const int edge = im / 8 > 3 ? im / 8 : 3;
+    const int ilo = edge, ihi = im - edge;
+    const int fpmin = fp_min > 1 ? fp_min : 1, fpmax = fp_max > fpmin ? fp_max : fpmin;
+    const long target = (long)std::ceil((double)coverage * im * jm);
+    long covered = 0;
+    for (int tries = 0; tries < 200000 && covered < target; ++tries) {
+      int wx = irange(fpmin, fpmax);
+      const int span = ihi - ilo > 1 ? ihi - ilo : 1;
+      if (wx > span) wx = span;
+      int wy = irange(fpmin, fpmax);
+      if (wy > jm) wy = jm;
+      const int i0 = irange(ilo, ihi - wx > ilo ? ihi - wx : ilo);
+      const int j0 = irange(1, jm);
+      const float ht = (float)(h_min + (h_max - h_min) * uni());
+      for (int jj = 0; jj < wy; ++jj)
+        for (int ii = 0; ii < wx; ++ii) {
+          const int i = i0 + ii, j = 1 + (j0 - 1 + jj) % jm;
+          if (i > ihi) continue;
+          float &z = zbm[(size_t)(i - 1) + (size_t)(j - 1) * im];
+          if (z <= 0.f) ++covered;
+          if (ht > z) z = ht;
+        }
+    }
+  }
+  double deg = std::fmod((double)direction, 360.0);
+  if (deg < 0) deg += 360.0;
+  const double r = deg - 90.0 * std::floor((deg + 45.0) / 90.0);
+  const double rr = r * 3.14159265358979323846 / 180.0;
+  const double cr = std::cos(rr), sr = std::sin(rr);
+  for (int k = 1; k <= km; ++k) {
+    double U = 5.0;  // bondv1.f95:33-54: 5 m/s (u(k>=79) = u(77) is 5 as well)
+    if (inflow_law != 0) {
+      const double z = (double)z2[k] + 0.5 * (double)dzn[k + 1];
+      U = (double)u_ref * std::pow(z / (double)z_ref, (double)pl_exp);
+    }
+    for (int j = 1; j <= jm; ++j) {
+      const size_t q = (size_t)(j - 1) + (size_t)(k - 1) * jm;
+      const double nu = noise * (2.0 * uni() - 1.0);
+      const double nv = noise * (2.0 * uni() - 1.0);
+      const double nw = noise * (2.0 * uni() - 1.0);
+      uin[q] = (float)(U * cr + nu);
+      vin[q] = (float)(U * sr + nv);
+      win[q] = (float)nw;
+    }
+  }
+  return 0;
+}
+
 int ref_set_threads(int n) {
 #ifdef _OPENMP
   if (n > 0) omp_set_num_threads(n);

@@ -67,6 +67,12 @@ void ref_diag(void *h, double *out);
 /* 1 if built with array bounds checks (mirrors gfortran -fbounds-check) */
 int ref_bounds_checked(void);
 const char *ref_last_error(void);
+/* The configs' seeded synthetic scenario (heightmap zbm(1:im,1:jm), inflow planes
+ * (1:jm,1:km)), restated so that the checker and the CPU baseline need nothing from the
+ * product.  fl[10] = {dz0, dz_ratio, coverage, h_min, h_max, u_ref, z_ref, pl_exp,
+ * direction_deg, noise}; in[4] = {dz_law, fp_min, fp_max, inflow_law}. */
+int ref_scenario(int im, int jm, int km, const float *fl, const int *in, unsigned long long seed, float *zbm,
+                 float *uin, float *vin, float *win);
 /* threads of the fast build's parallel loops from now on (n > 0), for the calling
  * thread; returns the number its next loops will use (1 in the serial builds) */
 int ref_set_threads(int n);

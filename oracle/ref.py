@@ -59,6 +59,8 @@ def load(fast: bool = False) -> C.CDLL:
     lib.ref_set_threads.argtypes = [C.c_int]
     lib.ref_trap_wall.restype = C.c_int
     lib.ref_trap_wall.argtypes = [vp, C.c_int]
+    lib.ref_scenario.restype = C.c_int
+    lib.ref_scenario.argtypes = [C.c_int] * 3 + [fp_, ip_, C.c_ulonglong, fp_, fp_, fp_, fp_]
     _libs[name] = lib
     return lib
 
@@ -68,6 +70,28 @@ def set_threads(n: int, fast: bool = True) -> int:
     the OpenMP runtime starts -- often at `import torch` -- so it cannot be relied on);
     returns the count the next steps use."""
     return int(load(fast).ref_set_threads(int(n)))
+
+
+def scenario(im: int, jm: int, km: int, seed: int = 1, *, dz_law: int = 1, dz0: float = 2.0,
+             dz_ratio: float = 1.04, coverage: float = 0.30, fp_min: int = 5, fp_max: int = 20,
+             h_min: float = 10.0, h_max: float = 60.0, inflow_law: int = 1, u_ref: float = 5.0,
+             z_ref: float = 100.0, pl_exp: float = 0.2, direction_deg: float = 0.0, noise: float = 1e-3,
+             fast: bool = False, **_ignored):
+    """The configs' seeded synthetic scenario as the oracle restates it: (zbm[im,jm],
+    uin[jm,km], vin, win), Fortran-ordered float32.  The defaults are the workload's
+    (30 % coverage of 5-20-cell blocks 10-60 m high, 5 m/s (z/100 m)^0.2 inflow with
+    +-1e-3 m/s noise, dz = 2 m x 1.04)."""
+    lib = load(fast)
+    fl = np.array([dz0, dz_ratio, coverage, h_min, h_max, u_ref, z_ref, pl_exp, direction_deg, noise], np.float32)
+    iv = np.array([dz_law, fp_min, fp_max, inflow_law], np.int32)
+    zbm = np.zeros((im, jm), np.float32, order="F")
+    uin, vin, win = (np.zeros((jm, km), np.float32, order="F") for _ in range(3))
+    f = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+    rc = lib.ref_scenario(im, jm, km, f(fl), iv.ctypes.data_as(C.POINTER(C.c_int)), C.c_ulonglong(seed), f(zbm),
+                          f(uin), f(vin), f(win))
+    if rc:
+        raise RuntimeError("ref_scenario: " + lib.ref_last_error().decode())
+    return zbm, uin, vin, win
 
 
 class Ref:

@@ -108,6 +108,28 @@ def test_scenario_generator_is_deterministic_and_in_range(built_lib):
     assert not np.array_equal(c[0], zbm)
 
 
+@pytest.mark.parametrize("kw", [
+    dict(im=60, jm=40, km=20, seed=5),
+    dict(im=150, jm=150, km=90, seed=1),
+    dict(im=96, jm=64, km=64, seed=123456789012, coverage=0.41, direction_deg=217.5, u_ref=7.3),
+    dict(im=64, jm=256, km=48, seed=77, inflow_law=0, coverage=0.15),
+    dict(im=80, jm=40, km=60, seed=9, dz_law=0, direction_deg=-30.0),
+    dict(im=32, jm=16, km=12, seed=3, coverage=0.0),
+])
+def test_oracle_scenario_is_the_products(built_lib, kw):
+    """The oracle's restatement of the scenario generator gives the product's arrays bit
+    for bit, so the CPU baseline and the checker build their inputs without the product."""
+    sc = lesgpu.Scenario(**kw)
+    a = lesgpu.generate_scenario(sc)
+    b = ref.scenario(**{k: getattr(sc, k) for k in ("im", "jm", "km", "seed", "dz_law", "dz0", "dz_ratio",
+                                                    "coverage", "fp_min", "fp_max", "h_min", "h_max",
+                                                    "inflow_law", "u_ref", "z_ref", "pl_exp", "direction_deg",
+                                                    "noise")})
+    for x, y in zip(a, b):
+        assert x.shape == y.shape
+        assert np.array_equal(x.view(np.uint32), y.view(np.uint32))
+
+
 def test_direction_rotates_inflow(built_lib):
     sc = scenario(40, 32, 20, seed=3, direction_deg=30.0, noise=0.0)
     _, uin, vin, _ = lesgpu.generate_scenario(sc)
