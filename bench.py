@@ -247,6 +247,38 @@ def run_reference(args):
     return 0
 
 
+def parity_check(im, jm, km, nsteps=5):
+    """A fresh domain of the benchmark's kind stepped nsteps times on the GPU and in the
+    FP64 oracle (the reference built with -freal-4-real-8, all host threads): the max
+    relative error max|x - x64| / max|x64| of the interior u, v, w, p (contract 1e-4)."""
+    import lesgpu
+    from oracle import ref as oref
+    sc = scenario(seed=1, im=im, jm=jm, km=km)
+    d = lesgpu.Domain(im, jm, km, lesgpu.Params())
+    d.setup_scenario(sc)
+    for n in range(1, nsteps + 1):
+        d.step(n, nsteps)
+    d.sync()
+    lo, hi = (1, 1, 1), (im, jm, km)
+    got = {nm: d.download(fid, lo, hi) for nm, fid in (("u", lesgpu.U), ("v", lesgpu.V), ("w", lesgpu.W),
+                                                        ("p", lesgpu.P))}
+    d.close()
+    t0 = time.perf_counter()
+    zbm, uin, vin, win = oref.scenario(im, jm, km, 1, fast=True)
+    threads = oref.set_threads(os.cpu_count() or 1)
+    r = oref.Ref(8, im, jm, km, zbm, uin, vin, win, sqrt_half=0, red64=1, fast=True)
+    for n in range(1, nsteps + 1):
+        r.step(n, nsteps)
+    errs = {}
+    for nm, fid in (("u", lesgpu.U), ("v", lesgpu.V), ("w", lesgpu.W), ("p", lesgpu.P)):
+        o = r.get(fid, lo, hi)
+        errs[nm] = float(abs(got[nm].astype("float64") - o).max() / max(float(abs(o).max()), 1e-30))
+    r.close()
+    return {"max_rel_err": max(errs.values()), "per_field": errs, "tolerance": 1e-4,
+            "against": f"FP64 oracle, {nsteps} steps of {im}x{jm}x{km} from rest, {threads} host threads, "
+                       f"{time.perf_counter() - t0:.1f} s"}
+
+
 def _seconds_synced(fn):
     t0 = time.perf_counter()
     fn()
@@ -451,6 +483,12 @@ def run_ours(args):
     dom.close()
 
     line = None
+    parity = None
+    if rank == 0 and not args.no_parity:
+        try:
+            parity = parity_check(IM, JM, KM)
+        except Exception as e:  # the check must not sink the GPU line
+            parity = {"failed": str(e)}
     if rank == 0:
         cpu = None
         if not args.no_cpu:
@@ -469,7 +507,8 @@ def run_ours(args):
                         "steps": e2e_steps,
                         "read_back": "les_gpu_download_async of interior u, v, w, p every step (snapshot in "
                                      "stream order, copy overlapping the next step), all waited for"},
-                "gpu_launches": launches, "nonfinite": bad, "roofline": roofline, "cpu_baseline": cpu}
+                "gpu_launches": launches, "nonfinite": bad, "roofline": roofline, "cpu_baseline": cpu,
+                "parity": parity}
         if not args.no_batch:
             try:
                 line["batched"], line["uneven"] = batched_lines()
@@ -570,6 +609,7 @@ def main():
     ap.add_argument("--dims", default=f"{IM}x{JM}x{KM}", help="domain IMxJMxKM (default: the workload's)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-ensemble measurements")
+    ap.add_argument("--no-parity", action="store_true", help="skip the FP64-oracle check of a short run")
     ap.add_argument("--sor-shape", default=None,
                     help="NXxNYxKCHUNK: fix the SOR tile shape instead of tuning it (for runs under a profiler, "
                          "whose timings would mislead the tuner)")
