@@ -476,6 +476,7 @@ def run_ours(args):
                 "traffic": (tpc * cells) if tpc else None, "ms_per_launch": sweep_ms,
                 "alg_bytes_per_launch": alg,
                 "sor_tile": {"nx": sor_shape[0], "ny": sor_shape[1], "kchunk": sor_shape[2],
+                             "depth": sor_shape[3],
                              "tuner_us": sor_tuned_us},
                 "stages_ms": stage_ms,
                 "step_alg_GBps": BYTES_PER_CELL_STEP * cells / (ms / args.steps / 1e3) / 1e9,
@@ -611,8 +612,8 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-ensemble measurements")
     ap.add_argument("--no-parity", action="store_true", help="skip the FP64-oracle check of a short run")
     ap.add_argument("--sor-shape", default=None,
-                    help="NXxNYxKCHUNK: fix the SOR tile shape instead of tuning it (for runs under a profiler, "
-                         "whose timings would mislead the tuner)")
+                    help="NXxNYxKCHUNK[xDEPTH]: fix the SOR tile shape (and iterations per k-march) instead of "
+                         "tuning it (for runs under a profiler, whose timings would mislead the tuner)")
     ap.add_argument("--mode", default="plain", choices=["plain", "serve"])
     ap.add_argument("--serve-seconds", type=float, default=120.0, help="serve mode: arrival window")
     ap.add_argument("--rate", type=float, default=20.0, help="serve mode: requests per second")

@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define LES_GPU_ABI_VERSION 1
+#define LES_GPU_ABI_VERSION 2
 
 /* status codes */
 #define LES_OK 0
@@ -309,30 +309,37 @@ int les_gpu_read_restart(les_handle *h, const char *data30, const char *data31, 
 
 /* Tile shape of press's fused SOR sweep.  nx: float4 columns per tile row, 32 (120
  * interior i cells) or 16 (56 cells, uniform cn1 only); ny: tile rows, 16/20/24/28
- * (ny - 4 interior j rows); kchunk: k planes per CTA (the march is split in k chunks
- * when kchunk < km).  0 leaves a value to the automatic choice.  The shape never
- * changes the fields, only the speed and the residual's summation order.
+ * (and 32 with depth 2); kchunk: k planes per CTA (the march is split in k chunks when
+ * kchunk < km); depth: SOR iterations per k-march, 1, or 2 (iteration l+1 trailing l by
+ * two planes in the same march, so p and rhs cross HBM once per two iterations; 32
+ * columns, ny 24/28/32, the whole march, omega = 1 and uniform x/y coefficients, else
+ * the sweep runs depth 1).  The interior j rows of a tile are ny - 4 depth.  0 leaves a
+ * value to the automatic choice.  The shape never changes the fields, only the speed
+ * and the residual's summation order; with the exit on sor < pjuge (press.f95:119-121)
+ * a two-iteration launch whose first iteration met the test is cut back to it.
  * les_gpu_set_sor_shape drops captured step graphs (the next step captures again);
- * les_gpu_sor_shape reports the shape in use, {0, 0, 0} for the per-subroutine SOR
- * (odd jm or km >= 511).  No reference counterpart: these are the tuning knobs. */
-int les_gpu_set_sor_shape(les_handle *h, int nx, int ny, int kchunk);
-int les_gpu_sor_shape(les_handle *h, int out[3]);
+ * les_gpu_sor_shape reports {nx, ny, kchunk, depth} in use, zeros for the
+ * per-subroutine SOR (odd jm or km >= 511).  No reference counterpart: these are the
+ * tuning knobs. */
+int les_gpu_set_sor_shape(les_handle *h, int nx, int ny, int kchunk, int depth);
+int les_gpu_sor_shape(les_handle *h, int out[4]);
 
-/* Autotuner of the SOR tile shape per size class (im, jm, km, and the device).  It
- * times the candidate shapes on scratch copies of this domain's SOR buffers: with
- * shared = 0 the domain alone on the GPU (tile heights x k chunks), with shared = 1
- * many replicas running at once, the way batch members share the GPU (16- and
- * 32-column tiles).  The fastest shape goes into a process-wide table that domains
+/* Autotuner of the SOR tile shape and fusion depth per size class (im, jm, km, and the
+ * device).  It times the candidate shapes on scratch copies of this domain's SOR
+ * buffers: with shared = 0 the domain alone on the GPU (tile heights x k chunks, and
+ * two-iteration marches), with shared = 1 many replicas running at once, the way batch
+ * members share the GPU (16- and 32-column tiles, and two-iteration marches).  The fastest shape goes into a process-wide table that domains
  * of the class use from their next step on (les_batch_add marks a member shared);
  * les_gpu_set_sor_shape still overrides it.  Run it while nothing else uses the GPU.
- * out (or NULL): the shape chosen, {0,0,0} when the domain has no fused sweep;
+ * out (or NULL): the shape chosen {nx, ny, kchunk, depth}, zeros when the domain has
+ * no fused sweep;
  * us (or NULL): its microseconds per SOR iteration and domain; report (or NULL): the
  * candidates' timings as text, truncated to len bytes.
  * les_sor_tuned reads the table (1: found, 0: not tuned); les_sor_set_tuned writes an
  * entry (e.g. from a saved table), nx = 0 erases it. */
-int les_gpu_tune_sor(les_handle *h, int shared, int out[3], double *us, char *report, size_t len);
-int les_sor_tuned(int im, int jm, int km, int shared, int device, int out[3]);
-int les_sor_set_tuned(int im, int jm, int km, int shared, int device, int nx, int ny, int kchunk);
+int les_gpu_tune_sor(les_handle *h, int shared, int out[4], double *us, char *report, size_t len);
+int les_sor_tuned(int im, int jm, int km, int shared, int device, int out[4]);
+int les_sor_set_tuned(int im, int jm, int km, int shared, int device, int nx, int ny, int kchunk, int depth);
 
 /* Profiling: queue `reps` back-to-back launches of one stage on the handle's stream,
  * bracketed by CUDA events, and return the average milliseconds per repetition.

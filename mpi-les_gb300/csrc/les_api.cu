@@ -158,7 +158,7 @@ int pitch_for(int im) { return ((im + 6) + 15) / 16 * 16; }
 }  // namespace
 
 extern "C" size_t les_domain_bytes(int im, int jm, int km) {
-  const size_t pi = (size_t)pitch_for(im), nj = (size_t)jm + 4, nk = (size_t)km + 4;
+  const size_t pi = (size_t)pitch_for(im), nj = (size_t)jm + 8, nk = (size_t)km + 4;
   const size_t field = pi * nj * nk * sizeof(float);
   const size_t part = ((size_t)(im + 63) / 64 + 1) * ((size_t)(jm + 3) / 4 + 1) * (size_t)km * 2 * sizeof(double);
   // deferred-block lists (les_gpu_create): FIX_COUNT lists over the largest grid of those kernels
@@ -180,7 +180,7 @@ extern "C" int les_gpu_create(const les_dims *dims, const les_params *params, le
   h->dims = *dims;
   h->prm = *params;
   h->pi = pitch_for(im);
-  h->nj = jm + 4;
+  h->nj = jm + 8;
   h->np = h->pi * h->nj;
   h->nfloat = (size_t)h->np * (size_t)(km + 4);
   if (h->nfloat >= (size_t)1 << 31) {
@@ -687,6 +687,16 @@ extern "C" int les_gpu_commit_setup(les_handle *h) {
     d.rhx = ok ? 1.f / P : 0.f; d.rhx2 = ok ? 1.f / (P + P) : 0.f;
     d.rhy = ok ? 1.f / Q : 0.f; d.rhy2 = ok ? 1.f / (Q + Q) : 0.f;
   }
+  {  // one value each for cn2l, cn2s, cn3l, cn3s: the two-iteration SOR sweep reads scalars
+    auto one = [&](int id) {
+      const std::vector<float> &v = h->h1d[id];
+      if (v.empty()) return false;
+      for (float x : v)
+        if (memcmp(&x, &v[0], sizeof(float)) != 0) return false;
+      return true;
+    };
+    d.sor_uni = (one(LES_FIELD_CN2L) && one(LES_FIELD_CN2S) && one(LES_FIELD_CN3L) && one(LES_FIELD_CN3S)) ? 1 : 0;
+  }
   {  // every divisor in [2^-20, 2^20]: reciprocal-corrected divisions (dvz)
     auto inr = [](float x) { const float a = std::fabs(x); return std::isfinite(x) && a >= 0x1p-20f && a <= 0x1p20f; };
     bool ok = inr(logz) && inr(h->prm.ro) && inr(h->prm.dt);
@@ -927,27 +937,33 @@ extern "C" int les_gpu_aveflow(les_handle *h, int n, int n1, int nmax) {
   return check_launch(h, "aveflow");
 }
 
-extern "C" int les_gpu_set_sor_shape(les_handle *h, int nx, int ny, int kchunk) {
+extern "C" int les_gpu_set_sor_shape(les_handle *h, int nx, int ny, int kchunk, int depth) {
   if (!h) return LES_ERR_ARG;
-  if ((nx != 0 && nx != 16 && nx != 32) || (ny != 0 && ny != 16 && ny != 20 && ny != 24 && ny != 28) || kchunk < 0)
-    return fail(h, LES_ERR_ARG, "set_sor_shape: nx in {0,16,32}, ny in {0,16,20,24,28}, kchunk >= 0");
+  if ((nx != 0 && nx != 16 && nx != 32) || (ny != 0 && ny != 16 && ny != 20 && ny != 24 && ny != 28 && ny != 32) ||
+      kchunk < 0 || depth < 0 || depth > 2)
+    return fail(h, LES_ERR_ARG, "set_sor_shape: nx in {0,16,32}, ny in {0,16,20,24,28,32}, kchunk >= 0, depth 0..2");
+  if (ny == 32 && depth != 2)
+    return fail(h, LES_ERR_ARG, "set_sor_shape: 32-row tiles run two iterations per march only (depth 2)");
+  if (depth == 2 && (nx == 16 || ny == 16 || ny == 20 || (kchunk > 0 && kchunk < h->dims.km)))
+    return fail(h, LES_ERR_ARG, "set_sor_shape: depth 2 takes 32-column tiles, ny 24/28/32 and the whole march");
   if (h->s) CK(h, cudaStreamSynchronize(h->s));
-  h->plan.fixed = SorShape{nx, ny, kchunk};
+  h->plan.fixed = SorShape{nx, ny, kchunk, depth};
   les_step_plan_free(&h->plan);  // the next step re-plans and captures its graphs again
   return LES_OK;
 }
 
-extern "C" int les_gpu_sor_shape(les_handle *h, int out[3]) {
+extern "C" int les_gpu_sor_shape(les_handle *h, int out[4]) {
   NEED_COMMIT(h);
   if (!out) return LES_ERR_ARG;
   const SorShape sh = les_step_plan_shape(h->dom, &h->plan);
   out[0] = sh.ny > 0 ? sh.nx : 0;
   out[1] = sh.ny;
   out[2] = sh.ny > 0 ? sh.kchunk : 0;
+  out[3] = sh.ny > 0 ? sh.depth : 0;
   return LES_OK;
 }
 
-extern "C" int les_gpu_tune_sor(les_handle *h, int shared, int out[3], double *us, char *report, size_t len) {
+extern "C" int les_gpu_tune_sor(les_handle *h, int shared, int out[4], double *us, char *report, size_t len) {
   NEED_COMMIT(h);
   CK(h, cudaSetDevice(h->dev));
   CK(h, cudaStreamSynchronize(h->s));
@@ -966,7 +982,7 @@ extern "C" int les_gpu_tune_sor(les_handle *h, int shared, int out[3], double *u
     report[n] = 0;
   }
   if (rc == 1) {  // odd jm or km too large: the per-subroutine SOR has no shape
-    if (out) out[0] = out[1] = out[2] = 0;
+    if (out) out[0] = out[1] = out[2] = out[3] = 0;
     if (us) *us = 0.0;
     return LES_OK;
   }
@@ -975,13 +991,14 @@ extern "C" int les_gpu_tune_sor(les_handle *h, int shared, int out[3], double *u
     out[0] = best.nx;
     out[1] = best.ny;
     out[2] = best.kchunk;
+    out[3] = best.depth;
   }
   if (us) *us = sec * 1e6;
   les_step_plan_free(&h->plan);  // re-plan with the tuned shape at the next step
   return LES_OK;
 }
 
-extern "C" int les_sor_tuned(int im, int jm, int km, int shared, int device, int out[3]) {
+extern "C" int les_sor_tuned(int im, int jm, int km, int shared, int device, int out[4]) {
   if (!out) return LES_ERR_ARG;
   int sms = 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
@@ -993,19 +1010,25 @@ extern "C" int les_sor_tuned(int im, int jm, int km, int shared, int device, int
   out[0] = sh.nx;
   out[1] = sh.ny;
   out[2] = sh.kchunk;
+  out[3] = sh.depth;
   return 1;
 }
 
-extern "C" int les_sor_set_tuned(int im, int jm, int km, int shared, int device, int nx, int ny, int kchunk) {
-  if (im < 1 || jm < 1 || km < 1 || (nx != 0 && nx != 16 && nx != 32) ||
-      (nx != 0 && ny != 16 && ny != 20 && ny != 24 && ny != 28) || kchunk < 0)
-    return LES_ERR_ARG;
+extern "C" int les_sor_set_tuned(int im, int jm, int km, int shared, int device, int nx, int ny, int kchunk,
+                                 int depth) {
+  if (im < 1 || jm < 1 || km < 1 || (nx != 0 && nx != 16 && nx != 32) || kchunk < 0) return LES_ERR_ARG;
+  if (nx != 0) {
+    if (ny != 16 && ny != 20 && ny != 24 && ny != 28 && ny != 32) return LES_ERR_ARG;
+    if (depth != 1 && depth != 2) return LES_ERR_ARG;
+    if (ny == 32 && depth != 2) return LES_ERR_ARG;  // 32-row tiles are built for depth 2 only
+    if (depth == 2 && (nx != 32 || ny < 24 || (kchunk > 0 && kchunk < km))) return LES_ERR_ARG;
+  }
   int sms = 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
     (void)cudaGetLastError();
     return LES_ERR_CUDA;
   }
-  les_tune_store(im, jm, km, shared, sms, SorShape{nx, ny, kchunk > 0 ? std::min(kchunk, km) : km});
+  les_tune_store(im, jm, km, shared, sms, SorShape{nx, ny, kchunk > 0 ? std::min(kchunk, km) : km, depth});
   return LES_OK;
 }
 

@@ -1,10 +1,11 @@
 // les_common.cuh -- device data layout and the face quantities of the MPI-LES stencils.
 //
 // Layout in HBM.  Every 3-D field of a domain uses one padded layout: i fastest,
-// then j rows, then k planes.  Logical indices cover i in [-3, pi-4], j in [-1, jm+2],
-// k in [-1, km+2], which holds every declared extent of src/main.f95:63-159.  The
-// interior cell i = 1 sits at column 4, so interior rows start 16-byte aligned and the
-// row pitch pi (floats) is a multiple of 16 (64 bytes).
+// then j rows, then k planes.  Logical indices cover i in [-3, pi-4], j in [-3, jm+4],
+// k in [-1, km+2], which holds every declared extent of src/main.f95:63-159 and the
+// four periodic ghost rows per side that the SOR sweep fusing two iterations reads.
+// The interior cell i = 1 sits at column 4, so interior rows start 16-byte aligned and
+// the row pitch pi (floats) is a multiple of 16 (64 bytes).
 //
 // Face quantities.  The reference's vel2 (src/vel2.f95:74-356) stores 27 temporary
 // arrays (nou1-9, diu1-9, cov1-9) that velFG and les then read.  Here nou and cov are
@@ -18,7 +19,7 @@
 #include <cstdint>
 
 #define LES_IOFF 3
-#define LES_JOFF 1
+#define LES_JOFF 3
 #define LES_KOFF 1
 
 // 1-D arrays, each pointer shifted so that the Fortran index addresses it directly.
@@ -47,7 +48,9 @@ enum {
   CT_CONVERGED = 0,  // SOR converged flag of the current press call
   CT_ITERS,          // SOR iterations run in the current press call
   CT_ERROR,          // set by a kernel whose bounded wait gave up (never expected)
-  CT_COUNT = 4
+  CT_REDO,           // a two-iteration SOR launch must be cut back to its first iteration
+  CT_LASTBUF,        // where the last SOR launch wrote p: 0 sorA, 1 sorB, 2 p
+  CT_COUNT = 8
 };
 
 // deferred-block lists, one per kernel that divides with dvz
@@ -80,6 +83,9 @@ struct LesDom {
   int xy_pow2;
   int zfast;
   float rro, rdt, rlogz;
+  // sor_uni: cn2l, cn2s, cn3l and cn3s each hold one value over i (j), so the two-
+  // iteration SOR sweep reads them as scalars
+  int sor_uni;
   // with xy_pow2: the one x spacing hx and y spacing hy, 1/hx, 1/(2 hx), 1/hy, 1/(2 hy)
   float hx, hy, rhx, rhx2, rhy, rhy2;
   // deferred-block lists of the kernels that use dvz (FIX_*): [0] count, [1] ticket of
@@ -94,6 +100,29 @@ struct LesDom {
 
 __host__ __device__ __forceinline__ int lix(const LesDom &d, int i, int j, int k) {
   return (k + LES_KOFF) * d.np + (j + LES_JOFF) * d.pi + (i + LES_IOFF);
+}
+
+// Periodic ghost rows of the SOR buffers: rows j in [-3, 0] and [jm+1, jm+4] hold row
+// 1 + (j-1) mod jm.  ghost_mask(j, jm) has bit b set when row j + m jm is such a ghost
+// row, for m = -2, -1, 1, 2 (b = 0..3): at most four (jm = 2), none for rows 5..jm-4.
+// for_ghost_rows(j, jm, mask, f) calls f(m jm) for each set bit.
+__host__ __device__ __forceinline__ unsigned ghost_mask(int j, int jm) {
+  unsigned g = 0;
+  const int ms[4] = {-2, -1, 1, 2};
+#pragma unroll
+  for (int b = 0; b < 4; ++b) {
+    const int t = j + ms[b] * jm;
+    if (t >= -3 && t <= jm + 4) g |= 1u << b;
+  }
+  return g;
+}
+template <class F>
+__host__ __device__ __forceinline__ void for_ghost_rows(int jm, unsigned mask, F f) {
+  if (!mask) return;
+  if (mask & 1u) f(-2 * jm);
+  if (mask & 2u) f(-jm);
+  if (mask & 4u) f(jm);
+  if (mask & 8u) f(2 * jm);
 }
 
 // x**0.5 of the reference (vel2.f95:56-63): IEEE sqrt.  gfortran calls powf(x,0.5),

@@ -326,7 +326,7 @@ inline dim3 reduce_grid(const LesDom &d) { return dim3((d.im + BX - 1) / BX, (d.
 // rhs of the cells of block (bx, by, bz) -- columns (i, j), planes bz*RKC+1 .. -- plus
 // its partial of sum(dx1*dy1*dzn*rhs) (press.f95:63-72).  dst: the rhs array (rhs =
 // d.rhs) or the SOR's internal rhs buffer, which also takes periodic ghost copies of
-// rows 1, 2, jm-1, jm in rows jm+1, jm+2, -1, 0.  ZF: reciprocal-corrected divisions;
+// rows 1..4 in rows jm+1..jm+4 and of rows jm-3..jm in rows -3..0 (ghost_rows).  ZF: reciprocal-corrected divisions;
 // a block that met a dividend outside their range is recomputed whole by the fixup
 // (rhs only reads u, v, w, f, g, h, so recomputing overwrites with the same cells).
 template <bool P2, bool ZF>
@@ -336,15 +336,7 @@ __device__ __forceinline__ void rhs_block(const LesDom &d, float *dst, int ghost
   const int i = min(i0, d.im), j = min(j0, d.jm);  // past the edge: the edge cell again, not stored
   const int ka = bz * RKC + 1, kb = min(ka + RKC - 1, d.km);
   const float axy = d.gr.dx1[i] * d.gr.dy1[j];
-  // periodic ghost copies of this row: 1 -> jm+1, 2 -> jm+2, jm-1 -> -1, jm -> 0
-  // (offsets from the row's own cell; 0 = none; jm = 2 gives two copies per row)
-  int go1 = 0, go2 = 0;
-  if (ghost) {
-    if (j == 1) go1 = d.jm * d.pi;
-    if (j == 2) go1 = d.jm * d.pi;
-    if (j == d.jm - 1) go2 = -d.jm * d.pi;
-    if (j == d.jm) go2 = -d.jm * d.pi;
-  }
+  const unsigned gmask = ghost ? ghost_mask(j, d.jm) : 0u;  // periodic ghost copies of this row
   unsigned bd = 0;
   PairSum acc;
   // the loads of plane k+1 are issued before plane k's arithmetic
@@ -356,8 +348,7 @@ __device__ __forceinline__ void rhs_block(const LesDom &d, float *dst, int ghost
     const float rr = rhs_comp<P2, ZF>(d, i, j, k, cur, bd);
     if (in) {
       dst[c] = rr;
-      if (go1) dst[c + go1] = rr;
-      if (go2) dst[c + go2] = rr;
+      for_ghost_rows(d.jm, gmask, [&](int off) { dst[c + off * d.pi] = rr; });
       acc.add(axy * d.gr.dzn[k] * rr);
     }
     cur = nxt;
@@ -444,6 +435,8 @@ inline unsigned sub_mean_blocks(const LesDom &d) { return (unsigned)((d.jm * d.k
 __global__ void k_sor_begin(LesDom d) {
   d.ctl[CT_CONVERGED] = 0;
   d.ctl[CT_ITERS] = 0;
+  d.ctl[CT_REDO] = 0;
+  d.ctl[CT_LASTBUF] = 2;
 }
 // one colour of one SOR iteration: nrd = 0 updates i+j+k odd, nrd = 1 even
 __global__ void __launch_bounds__(BX *BY) k_sor_colour(LesDom d, int nrd, int nblk) {

@@ -53,13 +53,12 @@
 
 namespace {
 
-// Copy the interior of the buffer the last executed iteration wrote back into p, when
-// the sweep stopped before its final (p-writing) iteration.
+// Copy the interior of the buffer the last executed launch wrote back into p, when the
+// sweep stopped before its final (p-writing) launch or ran a single iteration.
 __global__ void k_sor_copyout(LesDom d, int nmaxp) {
-  const int it = d.ctl[CT_ITERS];
-  if (it >= nmaxp && nmaxp > 1) return;  // the last iteration wrote p itself
-  if (it < 1) return;
-  const float *src = (it & 1) ? d.sorB : d.sorA;
+  (void)nmaxp;
+  if (d.ctl[CT_ITERS] < 1 || d.ctl[CT_LASTBUF] == 2) return;  // nothing ran, or p was written
+  const float *src = (d.ctl[CT_LASTBUF] == 1) ? d.sorB : d.sorA;
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int j = blockIdx.y + 1;
   if (i > d.im) return;
@@ -83,7 +82,7 @@ void launch_tma(const LesDom &d, const SorArgs &a, const CUtensorMap &tp, const 
 }  // namespace
 
 int les_sor_fused_tiles(int im, int jm, SorShape sh) {
-  const int ti = 4 * sh.nx - 8, tj = sh.ny - 4;
+  const int ti = 4 * sh.nx - 8, tj = sh.ny - 4 * (sh.depth == 2 ? 2 : 1);
   return ((im + ti - 1) / ti) * ((jm + tj - 1) / tj);
 }
 
@@ -166,6 +165,10 @@ void les_launch_sor_iter(const LesDom &d, const SorArgs &a, SorShape sh, const L
                    cn1mode == 0 && d.omega == 1.f && (a.psrc == d.sorA || a.psrc == d.sorB);
   const CUtensorMap *tp = tma ? ((a.psrc == d.sorA) ? &maps->m[0] : &maps->m[1]) : nullptr;
   const CUtensorMap *tr = tma ? &maps->m[2] : nullptr;
+  if (a.depth == 2) {  // the caller checked les_sor_two_ok
+    les_launch_sor_iter2(d, a, sh.ny, *tp, *tr, s);
+    return;
+  }
   if (sh.nx == 16) {
     les_launch_sor_iter_nx16(d, a, sh.ny, tp, tr, s);
     return;
@@ -184,6 +187,17 @@ void les_launch_sor_iter(const LesDom &d, const SorArgs &a, SorShape sh, const L
     case 28: launch_reg<28>(d, a, cn1mode, s); break;
     default: launch_reg<24>(d, a, cn1mode, s); break;
   }
+}
+
+void les_launch_sor_redo(const LesDom &d, const SorArgs &two, cudaStream_t s) {
+  SorArgs a = two;
+  a.redo = 1;
+  a.depth = 1;
+  a.tj = 24 - 4;
+  a.kchunk = d.km;
+  a.nchunk = 1;
+  a.ntiles = les_sor_fused_tiles(d.im, d.jm, SorShape{32, 24, 0, 1});
+  launch_reg_kc<32, 24, false>(d, a, 0, s);
 }
 
 void les_launch_sor_copyout(const LesDom &d, int nmaxp, cudaStream_t s) {

@@ -19,13 +19,19 @@ struct SorArgs {
   int ghost;             // 1: also write pdst's periodic ghost rows (internal buffers)
   int kchunk;            // k planes per CTA (grid z = nchunk chunks); >= km: one chunk
   int nchunk;            // chunks (grid z)
+  int depth = 1;         // iterations this launch performs (1, or 2: les_sor2.cu)
+  int redo = 0;          // 1: recompute one iteration only if CT_REDO is set (after a
+                         // two-iteration launch whose first iteration met the exit test)
+  int dstcode = 0;       // where pdst is, for the copy-out: 0 sorA, 1 sorB, 2 p itself
 };
 
 // Tile shape of the fused sweep: nx float4 columns (32 or 16; the interior i cells per
-// tile are 4 nx - 8) by ny rows (the interior j rows are ny - 4), and kchunk k planes
-// per CTA (>= km: the whole march).  ny == 0 selects the per-subroutine path instead.
+// tile are 4 nx - 8) by ny rows, kchunk k planes per CTA (>= km: the whole march), and
+// the iterations fused into one k-march (depth 1; or 2: 32-column tiles, ny 24/28/32,
+// the whole march).  The interior j rows of a tile are ny - 4 depth.  ny == 0 selects
+// the per-subroutine path instead.
 struct SorShape {
-  int nx = 0, ny = 0, kchunk = 0;
+  int nx = 0, ny = 0, kchunk = 0, depth = 1;
 };
 
 // Tensor maps of the internal buffers (sorA, sorB, sorR) for one tile shape.
@@ -44,10 +50,21 @@ SorShape les_sor_pick_shape(int im, int jm, int sms, bool shared_gpu);
 int les_sor_pick_kchunk(int tiles, int km, int sms);
 int les_sor_make_maps(const LesDom &d, SorShape sh, LesSorMaps *maps);
 // One SOR iteration: the TMA kernel when the source is an internal buffer with valid
-// maps and cn1 is uniform, the register kernel otherwise.
+// maps and cn1 is uniform, the register kernel otherwise.  With a.depth == 2 (only when
+// les_sor_two_ok holds): two iterations in one launch (les_sor2.cu).
 void les_launch_sor_iter(const LesDom &d, const SorArgs &a, SorShape sh, const LesSorMaps *maps, cudaStream_t s);
+// Whether shape sh can run two iterations per launch on this domain from internal
+// buffers: 32-column tiles, ny 24/28/32, the whole march, omega = 1, a cn1 uniform in i
+// and j, and x and y coefficients cn2l, cn2s, cn3l, cn3s each one value (sor_uni).
+bool les_sor_two_ok(const LesDom &d, SorShape sh);
+void les_launch_sor_iter2(const LesDom &d, const SorArgs &a, int ny, const CUtensorMap &tp, const CUtensorMap &tr,
+                          cudaStream_t s);
 // 16-column tiles (les_sor16.cu): the TMA kernel when tp and tr are given, the register
 // kernel (uniform cn1, one k chunk) otherwise.
 void les_launch_sor_iter_nx16(const LesDom &d, const SorArgs &a, int ny, const CUtensorMap *tp,
                               const CUtensorMap *tr, cudaStream_t s);
 void les_launch_sor_copyout(const LesDom &d, int nmaxp, cudaStream_t s);
+// After a two-iteration launch `two` (sor_fixed == 0): recompute its first iteration
+// alone, from the same source into the same destination, if that iteration met the
+// exit test (CT_REDO); otherwise the launch returns at once.
+void les_launch_sor_redo(const LesDom &d, const SorArgs &two, cudaStream_t s);

@@ -102,13 +102,12 @@ __device__ __forceinline__ float relax_pair_m(int q, float4 &cur, float pl, floa
 }
 
 // Per-thread geometry shared by both kernels.
-constexpr int NO_GHOST = -1000;
 struct Lane {
   int c4, r, ib, jr, jw;
   bool row_owned, row_red, col_owned, owned, west0;
   int east_e;
   bool ival[4];
-  int ghost1, ghost2;  // periodic ghost rows that copy row jr (NO_GHOST: none)
+  unsigned gmask;  // ghost rows that copy row jr (ghost_mask)
 };
 
 template <int NX>
@@ -134,10 +133,7 @@ __device__ __forceinline__ Lane make_lane(const LesDom &d, int tj, int ny) {
   L.east_e = d.im - L.ib;
 #pragma unroll
   for (int e = 0; e < 4; ++e) L.ival[e] = (L.ib + e >= 1) && (L.ib + e <= d.im);
-  // row 1 -> jm+1, row 2 -> jm+2, row jm-1 -> -1, row jm -> 0 (jm = 2: two ghosts per row)
-  const int jm = d.jm;
-  L.ghost1 = (L.jr == 1) ? jm + 1 : (L.jr == 2) ? jm + 2 : NO_GHOST;
-  L.ghost2 = (L.jr == jm - 1) ? -1 : (L.jr == jm) ? 0 : NO_GHOST;
+  L.gmask = ghost_mask(L.jr, d.jm);
   return L;
 }
 
@@ -156,10 +152,7 @@ __device__ __forceinline__ void store_final(const LesDom &d, const SorArgs &a, c
     }
   };
   put(L.jr);
-  if (a.ghost) {
-    if (L.ghost1 != NO_GHOST) put(L.ghost1);
-    if (L.ghost2 != NO_GHOST) put(L.ghost2);
-  }
+  if (a.ghost) for_ghost_rows(d.jm, L.gmask, [&](int off) { put(L.jr + off); });
 }
 
 // FP32 (Kahan) per thread -> FP64 per CTA -> last CTA sums the CTA partials in order.
@@ -183,6 +176,13 @@ __device__ __forceinline__ void finish_residual(const LesDom &d, const SorArgs &
     *last = (ticket == (unsigned)(a.ntiles - 1));
   }
   __syncthreads();
+  if (*last && a.redo) {  // a recomputed first iteration: its residual is already recorded
+    if (tid == 0) {
+      d.ctl[CT_REDO] = 0;
+      *a.counter = 0u;
+    }
+    return;
+  }
   if (*last) {
     __threadfence();
     double t = 0.0;
@@ -195,6 +195,7 @@ __device__ __forceinline__ void finish_residual(const LesDom &d, const SorArgs &
       for (int q = 0; q < NW; ++q) tot += warp[q];
       d.scal[SC_SOR] = tot;
       d.ctl[CT_ITERS] += 1;
+      d.ctl[CT_LASTBUF] = a.dstcode;
       if (!d.sor_fixed && tot < (double)d.pjuge) d.ctl[CT_CONVERGED] = 1;
       *a.counter = 0u;
     }
@@ -221,7 +222,9 @@ __global__ void __launch_bounds__(NX *NY, min_ctas(NX)) k_sor_reg(LesDom d, SorA
   __shared__ float sC4l[LES_SOR_KMAX], sC4s[LES_SOR_KMAX], sCk[LES_SOR_KMAX];
   __shared__ double sWarp[NX * NY / 32];
   __shared__ int sLast;
-  if (d.ctl[CT_CONVERGED]) return;  // early exit of press.f95:119-121
+  // early exit of press.f95:119-121; in redo mode: run only when a two-iteration launch
+  // must be cut back to its first iteration
+  if (a.redo ? d.ctl[CT_REDO] == 0 : d.ctl[CT_CONVERGED] != 0) return;
 
   const Lane L = make_lane<NX>(d, a.tj, NY);
   const int c4 = L.c4, r = L.r, ib = L.ib, jw = L.jw;
@@ -450,7 +453,9 @@ __global__ void __launch_bounds__(NX *NY, min_ctas(NX))
     k_sor_tma(LesDom d, SorArgs a, const __grid_constant__ CUtensorMap tmP, const __grid_constant__ CUtensorMap tmR) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   TmaSmem<NX, NY, D> &S = *reinterpret_cast<TmaSmem<NX, NY, D> *>(smem_raw);
-  if (d.ctl[CT_CONVERGED]) return;  // early exit of press.f95:119-121
+  // early exit of press.f95:119-121; in redo mode: run only when a two-iteration launch
+  // must be cut back to its first iteration
+  if (a.redo ? d.ctl[CT_REDO] == 0 : d.ctl[CT_CONVERGED] != 0) return;
 
   const Lane L = make_lane<NX>(d, a.tj, NY);
   const int c4 = L.c4, r = L.r, ib = L.ib, jw = L.jw;
@@ -467,7 +472,7 @@ __global__ void __launch_bounds__(NX *NY, min_ctas(NX))
   constexpr float omega = 1.f;
   const bool producer = (r == 0) && (c4 == 0);
   const int tx = blockIdx.x * tile_i(NX);  // padded column of i0 - 4
-  const int ty = blockIdx.y * a.tj; // padded row of j0 - 2
+  const int ty = blockIdx.y * a.tj + (LES_JOFF - 1);  // padded row of j0 - 2
   const uint32_t stage_bytes = 2u * NY * NX * 16u;
   // this CTA's k chunk [ka, kb], marched from ka-1 (a red ring plane) to kb+1; it
   // loads planes mfirst .. mlast, plane m into stage (m - mfirst) % D

@@ -24,6 +24,10 @@ int les_step_parts_needed(int im, int jm, int km, int sms) {
       const int parts = t * ((km + kc - 1) / kc);
       worst = parts > worst ? parts : worst;
     }
+  for (int ny = 24; ny <= 32; ny += 4) {  // two-iteration marches: two partials per tile
+    const int parts = 2 * les_sor_fused_tiles(im, jm, SorShape{32, ny, km, 2});
+    worst = parts > worst ? parts : worst;
+  }
   return worst + 64;
 }
 
@@ -45,14 +49,18 @@ SorShape les_step_pick_shape(const LesDom &d) {
   SorShape sh;
   // a measured shape for the size class (les_tune_sor), else the model's choice
   if (!les_tune_lookup(d.im, d.jm, d.km, d.sor_ksplit != 0, sms, &sh)) sh = les_sor_pick_shape(d.im, d.jm, sms, d.sor_ksplit != 0);
-  // A/B measurements: LES_SOR_NX (32, 16), LES_SOR_NY (16, 20, 24, 28)
+  // A/B measurements: LES_SOR_NX (32, 16), LES_SOR_NY (16, 20, 24, 28, 32), LES_SOR_DEPTH (1, 2)
   if (const char *e = getenv("LES_SOR_NX")) {
     const int v = atoi(e);
     if (v == 16 || v == 32) sh.nx = v;
   }
   if (const char *e = getenv("LES_SOR_NY")) {
     const int v = atoi(e);
-    if (v == 16 || v == 20 || v == 24 || v == 28) sh.ny = v;
+    if (v == 16 || v == 20 || v == 24 || v == 28 || v == 32) sh.ny = v;
+  }
+  if (const char *e = getenv("LES_SOR_DEPTH")) {
+    const int v = atoi(e);
+    if (v == 1 || v == 2) sh.depth = v;
   }
   if (!d.gr.cn1k) sh.nx = 32;  // 16-column tiles are built for a uniform cn1 only
   return sh;
@@ -64,6 +72,18 @@ static void plan_pick(const LesDom &d, LesStepPlan *plan) {
   if (sh.ny > 0) {
     if (plan->fixed.nx && (plan->fixed.nx == 32 || d.gr.cn1k)) sh.nx = plan->fixed.nx;
     if (plan->fixed.ny) sh.ny = plan->fixed.ny;
+    if (plan->fixed.depth) sh.depth = plan->fixed.depth;
+    // two iterations per march: the whole march, where the domain allows it and its
+    // partials fit; else one iteration per launch (32-row tiles exist for depth 2 only)
+    if (sh.depth == 2) {
+      SorShape two = sh;
+      two.kchunk = d.km;
+      if (!les_sor_two_ok(d, two) ||
+          (plan->part_cap > 0 && 2LL * les_sor_fused_tiles(d.im, d.jm, two) > plan->part_cap))
+        sh.depth = 1;
+    }
+    if (sh.depth != 2) sh.depth = 1;
+    if (sh.depth == 1 && sh.ny == 32) sh.ny = 28;
     const int tiles = les_sor_fused_tiles(d.im, d.jm, sh);
     // k chunks: fixed by the caller, else tuned for the class, else (alone on the GPU,
     // 32-column tiles) enough to fill the SMs
@@ -73,6 +93,7 @@ static void plan_pick(const LesDom &d, LesStepPlan *plan) {
     else if (sh.nx == 32 && !d.sor_ksplit) kc = les_sor_pick_kchunk(tiles, d.km, d.sms > 0 ? d.sms : 152);
     kc = kc < 1 ? 1 : (kc > d.km ? d.km : kc);
     if (plan->part_cap > 0 && (long long)tiles * ((d.km + kc - 1) / kc) > plan->part_cap) kc = d.km;
+    if (sh.depth == 2) kc = d.km;
     sh.kchunk = kc;
   }
   plan->sor = sh;
@@ -86,35 +107,56 @@ SorShape les_step_plan_shape(const LesDom &d, LesStepPlan *plan) {
   return plan->sor;
 }
 
-// Iteration l reads p (l = 1) or the internal buffer iteration l-1 wrote, and writes
-// the internal buffer X(l) (X = sorB for odd l, sorA for even l) or, for the last
-// iteration, p itself.  A copy-out moves the result into p when the sweep stopped
-// early (press.f95:119) or ran a single iteration.
-// ev_first / ev_last (optional) are recorded after the first and after the last sweep.
+// Iteration 1 reads p and writes sorB; each later launch (one iteration, or two with
+// sh.depth == 2) reads the buffer the previous launch wrote and writes the other one,
+// or, for the launch that ends with iteration nmaxp, p itself.  A copy-out moves the
+// result into p when the sweep stopped early (press.f95:119) or ran a single
+// iteration.  With the exit test on, each two-iteration launch is followed by a redo
+// launch that cuts it back to its first iteration if that one met the test.
+// ev_first / ev_last (optional) are recorded after the first and after the last launch.
 static void enqueue_sor_fused(const LesDom &d, const les_params &prm, SorShape sh, const LesSorMaps *maps,
                               LesCtx ctx, cudaEvent_t ev_first = nullptr, cudaEvent_t ev_last = nullptr) {
   les_launch_sor_begin(d, ctx);
   const int nit = prm.nmaxp;
-  const int tiles = les_sor_fused_tiles(d.im, d.jm, sh);
-  const int kchunk = sh.kchunk > 0 ? sh.kchunk : d.km;
-  const int nchunk = (d.km + kchunk - 1) / kchunk;
-  for (int l = 1; l <= nit; ++l) {
+  SorShape one = sh;
+  one.depth = 1;
+  if (one.ny == 32) one.ny = 28;
+  const bool two_ok = sh.depth == 2 && maps && maps->valid && les_sor_two_ok(d, sh);
+  const float *cur = d.p;
+  for (int l = 1; l <= nit;) {
+    const bool two = two_ok && l >= 2 && l + 1 <= nit;
+    const SorShape &use = two ? sh : one;
+    const int lend = two ? l + 1 : l;
+    const int tiles = les_sor_fused_tiles(d.im, d.jm, use);
+    const int kchunk = (!two && use.kchunk > 0) ? use.kchunk : d.km;
+    const int nchunk = (d.km + kchunk - 1) / kchunk;
     SorArgs a;
-    a.psrc = (l == 1) ? d.p : (((l - 1) & 1) ? d.sorB : d.sorA);
-    const bool last = (l == nit) && (nit > 1);
-    a.pdst = last ? d.p : ((l & 1) ? d.sorB : d.sorA);
+    a.psrc = cur;
+    const bool last = (lend == nit) && (nit > 1);
+    a.pdst = last ? d.p : ((cur == d.sorB) ? d.sorA : d.sorB);
+    a.dstcode = last ? 2 : (a.pdst == d.sorA ? 0 : 1);
     a.ghost = last ? 0 : 1;
     a.rhs = d.sorR;
-    a.tj = sh.ny - 4;
+    a.depth = two ? 2 : 1;
+    a.tj = use.ny - 4 * a.depth;
     a.kchunk = kchunk;
     a.nchunk = nchunk;
     a.ntiles = tiles * nchunk;
     a.part = d.part;
     a.counter = d.cnt;
-    les_launch_sor_iter(d, a, sh, maps, ctx.s);
+    // a one-iteration launch on a depth-2 plan takes the maps' tile height only if it
+    // has a one-iteration kernel (not ny = 32: then the register kernel runs)
+    les_launch_sor_iter(d, a, (two || maps == nullptr || maps->shape.ny == one.ny) ? use : one,
+                        (two || (maps && maps->shape.ny == one.ny)) ? maps : nullptr, ctx.s);
     ++*ctx.nlaunch;
+    if (two && !prm.sor_fixed) {
+      les_launch_sor_redo(d, a, ctx.s);
+      ++*ctx.nlaunch;
+    }
     if (l == 1 && ev_first) cudaEventRecord(ev_first, ctx.s);
-    if (l == nit && ev_last) cudaEventRecord(ev_last, ctx.s);
+    if (lend == nit && ev_last) cudaEventRecord(ev_last, ctx.s);
+    cur = a.pdst;
+    l = lend + 1;
   }
   les_launch_sor_copyout(d, nit, ctx.s);
   ++*ctx.nlaunch;

@@ -14,7 +14,7 @@ struct LesStepPlan {
   SorShape sor;                    // fused SOR tile shape (sor.ny == 0: per-subroutine path)
   int sor_picked = 0;              // sor chosen (and maps made) for this plan
   LesSorMaps maps;                 // tensor maps of the SOR buffers for sor
-  SorShape fixed;                  // caller's choice (les_gpu_set_sor_shape), 0 = automatic;
+  SorShape fixed{0, 0, 0, 0};      // caller's choice (les_gpu_set_sor_shape), 0 = automatic;
                                    // kept across les_step_plan_free
   long long part_cap = 0;          // residual partials the domain's buffer holds
 };

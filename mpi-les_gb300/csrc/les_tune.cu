@@ -61,6 +61,11 @@ std::vector<SorShape> candidates(const LesDom &d, bool shared) {
         last = kc;
       }
     }
+  // two iterations per k-march (les_sor2.cu): 32-column tiles, the whole march
+  for (int ny : {24, 28, 32}) {
+    const SorShape two{32, ny, d.km, 2};
+    if (les_sor_two_ok(d, two)) c.push_back(two);
+  }
   return c;
 }
 
@@ -129,7 +134,8 @@ int time_shape(Scratch &S, SorShape sh, int iters, int reps, cudaStream_t s0, do
   const int tiles = les_sor_fused_tiles(S.dom[0].im, S.dom[0].jm, sh);
   const int kc = sh.kchunk > 0 ? sh.kchunk : S.dom[0].km;
   const int nch = (S.dom[0].km + kc - 1) / kc;
-  if ((size_t)tiles * nch > S.npart) return -2;
+  const int per = (sh.depth == 2) ? 2 : 1;  // iterations per launch
+  if ((size_t)tiles * nch * per > S.npart) return -2;
   cudaEvent_t fork, t0, t1;
   std::vector<cudaEvent_t> join(R);
   cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
@@ -145,13 +151,14 @@ int time_shape(Scratch &S, SorShape sh, int iters, int reps, cudaStream_t s0, do
     for (int r = 0; r < R; ++r) {
       cudaStreamWaitEvent(S.st[r], fork, 0);
       const LesDom &d = S.dom[r];
-      for (int l = 0; l < iters; ++l) {
+      for (int l = 0; l < iters; l += per) {
         SorArgs a;
-        a.psrc = (l & 1) ? d.sorB : d.sorA;
-        a.pdst = (l & 1) ? d.sorA : d.sorB;
+        a.psrc = ((l / per) & 1) ? d.sorB : d.sorA;
+        a.pdst = ((l / per) & 1) ? d.sorA : d.sorB;
         a.ghost = 1;
         a.rhs = d.sorR;
-        a.tj = sh.ny - 4;
+        a.depth = per;
+        a.tj = sh.ny - 4 * per;
         a.kchunk = kc;
         a.nchunk = nch;
         a.ntiles = tiles * nch;
@@ -215,7 +222,7 @@ int les_tune_sor(const LesDom &d, bool shared, size_t mem_budget, SorShape *best
   int min_tiles = 1 << 30;
   for (const SorShape &c : cands) {
     const int t = les_sor_fused_tiles(d.im, d.jm, c);
-    npart = std::max(npart, (size_t)t * (size_t)((d.km + c.kchunk - 1) / c.kchunk) + 64);
+    npart = std::max(npart, (size_t)t * (size_t)((d.km + c.kchunk - 1) / c.kchunk) * (size_t)c.depth + 64);
     min_tiles = std::min(min_tiles, t);
   }
   // batch members: about four waves of two CTAs per SM, within the memory budget
@@ -244,7 +251,8 @@ int les_tune_sor(const LesDom &d, bool shared, size_t mem_budget, SorShape *best
     rc = time_shape(S, c, iters, 3, s0, &sec);
     if (rc) break;
     if (report) {
-      snprintf(line, sizeof line, "  nx=%d ny=%d kchunk=%d: %.2f us\n", c.nx, c.ny, c.kchunk, sec * 1e6);
+      snprintf(line, sizeof line, "  nx=%d ny=%d kchunk=%d depth=%d: %.2f us\n", c.nx, c.ny, c.kchunk, c.depth,
+               sec * 1e6);
       *report += line;
     }
     if (sec < *best_sec) {

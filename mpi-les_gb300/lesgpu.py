@@ -196,13 +196,13 @@ def load_library(path: str | None = None) -> C.CDLL:
         "les_gpu_launch_count": (C.c_longlong, [vp]),
         "les_gpu_last_error": (C.c_int, [vp, C.c_char_p, C.c_size_t]),
         "les_gpu_profile": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(C.c_double)]),
-        "les_gpu_set_sor_shape": (C.c_int, [vp, C.c_int, C.c_int, C.c_int]),
+        "les_gpu_set_sor_shape": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int]),
         "les_gpu_aveflow": (C.c_int, [vp, C.c_int, C.c_int, C.c_int]),
         "les_gpu_sor_shape": (C.c_int, [vp, C.POINTER(C.c_int)]),
         "les_gpu_tune_sor": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double), C.c_char_p,
                                        C.c_size_t]),
         "les_sor_tuned": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int)]),
-        "les_sor_set_tuned": (C.c_int, [C.c_int] * 8),
+        "les_sor_set_tuned": (C.c_int, [C.c_int] * 9),
         "les_gpu_write_data20": (C.c_int, [vp, C.c_char_p, C.c_int]),
         "les_gpu_write_data21": (C.c_int, [vp, C.c_char_p, C.c_int]),
         "les_gpu_write_data30": (C.c_int, [vp, C.c_char_p, C.c_int, C.c_float, C.c_int]),
@@ -281,18 +281,20 @@ class LesError(RuntimeError):
 
 
 def sor_tuned(im: int, jm: int, km: int, shared: bool, device: int = 0):
-    """The tuned SOR shape (nx, ny, kchunk) of a size class, or None if it was never tuned."""
-    out = (C.c_int * 3)()
+    """The tuned SOR shape (nx, ny, kchunk, depth) of a size class, or None if it was
+    never tuned."""
+    out = (C.c_int * 4)()
     rc = load_library().les_sor_tuned(im, jm, km, 1 if shared else 0, device, out)
     if rc < 0:
         raise LesError(f"les_sor_tuned: {ERRORS.get(rc, rc)}")
-    return (int(out[0]), int(out[1]), int(out[2])) if rc == 1 else None
+    return tuple(int(x) for x in out) if rc == 1 else None
 
 
 def set_sor_tuned(im: int, jm: int, km: int, shared: bool, shape, device: int = 0) -> None:
-    """Enter (or with shape None erase) a size class's SOR shape in the tuned table."""
-    nx, ny, kc = shape if shape else (0, 0, 0)
-    rc = load_library().les_sor_set_tuned(im, jm, km, 1 if shared else 0, device, nx, ny, kc)
+    """Enter (or with shape None erase) a size class's SOR shape (nx, ny, kchunk[, depth])
+    in the tuned table."""
+    nx, ny, kc, depth = (tuple(shape) + (1,))[:4] if shape else (0, 0, 0, 0)
+    rc = load_library().les_sor_set_tuned(im, jm, km, 1 if shared else 0, device, nx, ny, kc, depth)
     if rc:
         raise LesError(f"les_sor_set_tuned: {ERRORS.get(rc, rc)}")
 
@@ -516,25 +518,27 @@ class Domain:
                                                   C.byref(n), C.byref(t)), "read_restart")
         return n.value, t.value
 
-    def set_sor_shape(self, nx: int = 0, ny: int = 0, kchunk: int = 0) -> None:
-        """Fix the SOR sweep's tile shape (0 = automatic); see les_gpu_set_sor_shape."""
-        self._check(self.lib.les_gpu_set_sor_shape(self._h, nx, ny, kchunk), "set_sor_shape")
+    def set_sor_shape(self, nx: int = 0, ny: int = 0, kchunk: int = 0, depth: int = 0) -> None:
+        """Fix the SOR sweep's tile shape and fusion depth (0 = automatic); see
+        les_gpu_set_sor_shape."""
+        self._check(self.lib.les_gpu_set_sor_shape(self._h, nx, ny, kchunk, depth), "set_sor_shape")
 
-    def sor_shape(self) -> tuple[int, int, int]:
-        """(nx, ny, kchunk) of the SOR sweep in use; (0, 0, 0) for the per-subroutine path."""
-        out = (C.c_int * 3)()
+    def sor_shape(self) -> tuple[int, int, int, int]:
+        """(nx, ny, kchunk, depth) of the SOR sweep in use; zeros for the per-subroutine path."""
+        out = (C.c_int * 4)()
         self._check(self.lib.les_gpu_sor_shape(self._h, out), "sor_shape")
-        return int(out[0]), int(out[1]), int(out[2])
+        return tuple(int(x) for x in out)
 
-    def tune_sor(self, shared: bool) -> tuple[tuple[int, int, int], float, str]:
-        """Time the SOR tile shapes for this domain's size class (alone, or sharing the
-        GPU with other domains), keep the fastest for the class; returns (shape,
-        microseconds per iteration, report of every candidate)."""
-        out = (C.c_int * 3)()
+    def tune_sor(self, shared: bool) -> tuple[tuple[int, int, int, int], float, str]:
+        """Time the SOR tile shapes and fusion depths for this domain's size class (alone,
+        or sharing the GPU with other domains), keep the fastest for the class; returns
+        (shape, microseconds per iteration, report of every candidate)."""
+        out = (C.c_int * 4)()
         us = C.c_double(0.0)
-        rep = C.create_string_buffer(8192)
-        self._check(self.lib.les_gpu_tune_sor(self._h, 1 if shared else 0, out, C.byref(us), rep, 8192), "tune_sor")
-        return (int(out[0]), int(out[1]), int(out[2])), us.value, rep.value.decode()
+        rep = C.create_string_buffer(16384)
+        self._check(self.lib.les_gpu_tune_sor(self._h, 1 if shared else 0, out, C.byref(us), rep, 16384),
+                    "tune_sor")
+        return tuple(int(x) for x in out), us.value, rep.value.decode()
 
     def profile(self, what: int, reps: int) -> float:
         """Average ms per repetition of one stage (it really runs and advances the state)."""

@@ -63,8 +63,8 @@ def test_batch_member_switches_to_narrow_sor_tiles(built_lib):
     assert d.sor_shape()[0] == 32
     b = lesgpu.Batch()
     b.add(d, 1, 1)
-    nx, ny, kchunk = d.sor_shape()
-    assert nx == 16 and kchunk == sc.km
+    nx, ny, kchunk, depth = d.sor_shape()
+    assert nx == 16 and kchunk == sc.km and depth == 1
     b.close()
 
 

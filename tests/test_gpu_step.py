@@ -102,26 +102,28 @@ def test_sor_k_chunks_match_one_chunk(built_lib, monkeypatch, kchunk):
 
 
 @pytest.mark.parametrize("shape", [(16, 16, 0), (16, 20, 0), (16, 24, 0), (16, 28, 0), (32, 20, 0), (32, 28, 5),
-                                   (16, 24, 5), (16, 28, 3)])
+                                   (16, 24, 5), (16, 28, 3), (32, 24, 0, 2), (32, 28, 0, 2), (32, 32, 0, 2)])
 def test_sor_tile_shapes_match(built_lib, shape):
     """Every tile shape of the fused SOR sweep -- 16- and 32-column tiles, each tile
-    height, k chunks of either -- gives the same fields bit for bit.  130 cells wide:
-    three 16-column tiles (the last one partial) against two 32-column ones."""
+    height, k chunks of either, and two iterations per k-march -- gives the same fields
+    bit for bit.  130 cells wide: three 16-column tiles (the last one partial) against
+    two 32-column ones; 36 rows: partial tiles in j for every height."""
     sc = scenario(130, 36, 14, seed=73)
     params = lesgpu.Params(nmaxp=9)
 
-    def run(nx, ny, kchunk):
+    def run(nx, ny, kchunk, depth=1):
         d = make_gpu(sc, params)
-        d.set_sor_shape(nx, ny, kchunk)
+        d.set_sor_shape(nx, ny, kchunk, depth)
         for n in range(1, 5):
             d.step(n, 4)
         d.sync()
         return d
 
-    a, b = run(32, 24, 1000), run(*shape)
-    assert a.sor_shape() == (32, 24, 14)
-    nx, ny, kchunk = shape
-    assert b.sor_shape() == (nx, ny, kchunk if kchunk else 14)
+    a, b = run(32, 24, 1000, 1), run(*shape)
+    assert a.sor_shape() == (32, 24, 14, 1)
+    nx, ny, kchunk = shape[:3]
+    depth = shape[3] if len(shape) > 3 else 1
+    assert b.sor_shape() == (nx, ny, kchunk if kchunk else 14, depth)
     for fid in lesgpu.STATE_FIELDS:
         x, y = a.download(fid), b.download(fid)
         assert np.array_equal(x.view(np.uint32), y.view(np.uint32)), (shape, lesgpu.FIELD_NAMES[fid])
@@ -132,9 +134,46 @@ def test_sor_tile_shapes_match(built_lib, shape):
 
 def test_sor_shape_rejects_unbuilt_shapes(built_lib):
     d = lesgpu.Domain(40, 20, 8, lesgpu.Params())
-    for bad in ((8, 24, 0), (32, 32, 0), (32, 24, -1)):
+    for bad in ((8, 24, 0), (32, 32, 0), (32, 24, -1), (32, 32, 0, 1), (16, 24, 0, 2), (32, 20, 0, 2),
+                (32, 24, 4, 2), (32, 24, 0, 3)):
         with pytest.raises(lesgpu.LesError):
             d.set_sor_shape(*bad)
+
+
+@pytest.mark.parametrize("nmaxp", [2, 3, 8, 9, 50])
+@pytest.mark.parametrize("shape", [(150, 60, 20), (64, 2, 12), (40, 4, 7)])
+def test_two_iteration_sor_matches_one_iteration(built_lib, nmaxp, shape):
+    """Two SOR iterations per k-march give the fields of one iteration per launch bit
+    for bit, for even and odd iteration counts (a one-iteration launch before or after
+    the pairs), partial tiles, jm = 2 and 4 (every ghost row a copy of a copy), and the
+    residual of the last iteration within summation-order rounding."""
+    sc = scenario(*shape, seed=75)
+    params = lesgpu.Params(nmaxp=nmaxp)
+
+    def run(depth):
+        d = make_gpu(sc, params)
+        d.set_sor_shape(32, 24 if depth == 1 else 28, 0, depth)
+        for n in range(1, 4):
+            d.step(n, 3)
+        d.sync()
+        return d
+
+    a, b = run(1), run(2)
+    assert b.sor_shape()[3] == 2
+    for fid in lesgpu.STATE_FIELDS:
+        x, y = a.download(fid), b.download(fid)
+        assert np.array_equal(x.view(np.uint32), y.view(np.uint32)), (nmaxp, lesgpu.FIELD_NAMES[fid])
+    da, db = a.diag(), b.diag()
+    assert da["iters"] == db["iters"] == nmaxp
+    assert abs(da["sor"] - db["sor"]) <= 1e-6 * abs(da["sor"])
+    # the per-subroutine press on the same plan gives the same fields as the graph step
+    c = make_gpu(sc, params)
+    c.set_sor_shape(32, 28, 0, 2)
+    for n in range(1, 4):
+        c.velnw(); c.bondv1(n); c.velfg(); c.feedbf(); c.les(); c.adam(); c.press(n, 3)
+    for fid in lesgpu.STATE_FIELDS:
+        x, y = b.download(fid), c.download(fid)
+        assert np.array_equal(x.view(np.uint32), y.view(np.uint32)), (nmaxp, lesgpu.FIELD_NAMES[fid])
 
 
 @pytest.mark.parametrize("spacing", [(4.0, 4.0), (3.0, 5.0)])
@@ -216,15 +255,20 @@ def test_steps_vs_committed_golden(built_lib):
     assert gpu.diag()["iters"] == int(g["diag32"][0])
 
 
+@pytest.mark.parametrize("depth", [1, 2])
 @pytest.mark.parametrize("pjuge,lo,hi", [(12000.0, 2, 48), (40000.0, 1, 6)])
-def test_sor_early_exit_like_the_reference(built_lib, pjuge, lo, hi):
+def test_sor_early_exit_like_the_reference(built_lib, pjuge, lo, hi, depth):
     """press.f95:119-121: the SOR loop exits once sor < pjuge.  With thresholds the
     residual crosses mid-loop (and after the first iteration), the whole-step graph
-    and the per-subroutine calls stop at the oracle's iteration in every step."""
+    and the per-subroutine calls stop at the oracle's iteration in every step -- also
+    when two iterations share a k-march and the first of them met the test (the launch
+    is cut back to it)."""
     sc = scenario(40, 24, 12, seed=5)
     params = lesgpu.Params(sor_fixed=0, pjuge=pjuge)
     gpu = make_gpu(sc, params)
     stages = make_gpu(sc, params)
+    for d in (gpu, stages):
+        d.set_sor_shape(32, 24 if depth == 1 else 28, 0, depth)
     orc = make_ref(4, sc, params, sqrt_half=1, red64=1)
     iters = []
     for n in range(1, 6):

@@ -35,10 +35,11 @@ def test_tune_alone_picks_a_timed_shape_and_keeps_fields(built_lib, clean_table)
     _steps(ref, 3)
     d = make_gpu(sc, params)
     shape, us, report = d.tune_sor(False)
-    nx, ny, kc = shape
-    assert nx in (16, 32) and ny in (16, 20, 24, 28) and 1 <= kc <= sc.km
-    assert us > 0 and f"nx={nx} ny={ny} kchunk={kc}:" in report
+    nx, ny, kc, depth = shape
+    assert nx in (16, 32) and ny in (16, 20, 24, 28, 32) and 1 <= kc <= sc.km and depth in (1, 2)
+    assert us > 0 and f"nx={nx} ny={ny} kchunk={kc} depth={depth}:" in report
     assert report.count("us\n") >= 8  # tile heights x k chunks were timed
+    assert "depth=2" in report  # and two-iteration marches
     assert lesgpu.sor_tuned(150, 60, 20, False) == shape
     assert lesgpu.sor_tuned(150, 60, 20, True) is None
     assert d.sor_shape() == shape
@@ -49,8 +50,8 @@ def test_tune_alone_picks_a_timed_shape_and_keeps_fields(built_lib, clean_table)
     # a new domain of the class starts with the tuned shape; a fixed shape still wins
     e = make_gpu(sc, params)
     assert e.sor_shape() == shape
-    e.set_sor_shape(32, 16, 0)
-    assert e.sor_shape()[:2] == (32, 16)
+    e.set_sor_shape(32, 16, 0, 1)
+    assert e.sor_shape()[:2] == (32, 16) and e.sor_shape()[3] == 1
 
 
 def test_tune_shared_steers_batch_members(built_lib, clean_table):
@@ -76,11 +77,14 @@ def test_tune_shared_steers_batch_members(built_lib, clean_table):
 
 def test_tune_without_fused_sweep_and_table_edits(built_lib, clean_table):
     d = make_gpu(scenario(40, 21, 8, seed=94), lesgpu.Params())  # odd jm: per-subroutine SOR
-    assert d.tune_sor(False)[0] == (0, 0, 0)
+    assert d.tune_sor(False)[0] == (0, 0, 0, 0)
     clean_table.append((70, 50, 30, True))
     lesgpu.set_sor_tuned(70, 50, 30, True, (16, 20, 0))
-    assert lesgpu.sor_tuned(70, 50, 30, True) == (16, 20, 30)
+    assert lesgpu.sor_tuned(70, 50, 30, True) == (16, 20, 30, 1)
+    lesgpu.set_sor_tuned(70, 50, 30, True, (32, 32, 0, 2))
+    assert lesgpu.sor_tuned(70, 50, 30, True) == (32, 32, 30, 2)
     lesgpu.set_sor_tuned(70, 50, 30, True, None)
     assert lesgpu.sor_tuned(70, 50, 30, True) is None
-    with pytest.raises(lesgpu.LesError):
-        lesgpu.set_sor_tuned(70, 50, 30, True, (24, 20, 0))
+    for bad in ((24, 20, 0), (32, 32, 0, 1), (16, 24, 0, 2), (32, 28, 10, 2)):
+        with pytest.raises(lesgpu.LesError):
+            lesgpu.set_sor_tuned(70, 50, 30, True, bad)
