@@ -373,6 +373,7 @@ def batched_lines(warmup=3, steps=10):
 
 def run_ours(args):
     world, rank, local, pg = dist_setup()
+    pool = oracle_pool() if (rank == 0 and not args.no_serve) else None  # FP64 checks of served requests
     import numpy as np
     import torch
     torch.cuda.set_device(local)
@@ -515,6 +516,12 @@ def run_ours(args):
                 line["batched"], line["uneven"] = batched_lines()
             except Exception as e:  # the ensembles must not sink the headline line
                 line["batched"] = {"failed": str(e)}
+        if not args.no_serve:
+            try:
+                line["serve"] = serve_lines(pool)
+            except Exception as e:  # the serving run must not sink the headline line
+                line["serve"] = {"failed": str(e)}
+            pool.close()
         print(json.dumps(line), flush=True)
     if pg is not None:
         pg.barrier()
@@ -523,78 +530,111 @@ def run_ours(args):
 
 
 def _oracle_check(job):
-    """FP64 oracle run of one served scenario (runs in a spawned worker process)."""
+    """FP64 oracle run of one served scenario to its final step (runs in a spawned
+    worker process; the scenario comes from the oracle's own generator): the max
+    relative error of the GPU's final u, v, w, p."""
     sc_kw, nsteps, gpu_fields = job
     import numpy as np
 
-    import lesgpu
     from oracle import ref as oref
     oref.set_threads(2)
-    sc = lesgpu.Scenario(**sc_kw)
-    zbm, uin, vin, win = lesgpu.generate_scenario(sc)
-    r = oref.Ref(8, sc.im, sc.jm, sc.km, zbm, uin, vin, win, dx=sc.dx, dy=sc.dy, dz_law=sc.dz_law, dz0=sc.dz0,
-                 dz_ratio=sc.dz_ratio, sqrt_half=0, red64=1, fast=True)
+    zbm, uin, vin, win = oref.scenario(fast=True, **sc_kw)
+    im, jm, km = sc_kw["im"], sc_kw["jm"], sc_kw["km"]
+    r = oref.Ref(8, im, jm, km, zbm, uin, vin, win, dx=sc_kw["dx"], dy=sc_kw["dy"], dz_law=sc_kw["dz_law"],
+                 dz0=sc_kw["dz0"], dz_ratio=sc_kw["dz_ratio"], sqrt_half=0, red64=1, fast=True)
     for n in range(1, nsteps + 1):
         r.step(n, nsteps)
     err = 0.0
     for fid, g in gpu_fields.items():
-        o = r.get(fid, (1, 1, 1), (sc.im, sc.jm, sc.km))
+        o = r.get(fid, (1, 1, 1), (im, jm, km))
         err = max(err, float(np.abs(g.astype(np.float64) - o).max() / max(np.abs(o).max(), 1e-30)))
     r.close()
     return err
 
 
-def run_serve(args):
-    """The serving stream: Poisson arrivals, admission by free HBM, continuous batching."""
-    import dataclasses
+def oracle_pool():
+    """Worker processes for the FP64 checks of served requests (spawned: safe after the
+    GPU is in use), two threads each over the host cores."""
     import multiprocessing as mp
+    return mp.get_context("spawn").Pool(processes=max(1, min(8, (os.cpu_count() or 2) // 2)))
 
-    # the oracle workers start before the first GPU call (spawn): the check runs after
-    mp_ctx = mp.get_context("spawn")
-    pool = mp_ctx.Pool(processes=max(1, min(8, (os.cpu_count() or 2) // 2)))
+
+def serve_window(rate, seconds, seed, pool, sample_every=20, max_check=None):
+    """One serving run: Poisson arrivals of wind scenarios at `rate` for `seconds`,
+    admission by free HBM, continuous batching.  Every `sample_every`-th request (5 %)
+    is checked against the FP64 oracle at its final step; the checks run on the host
+    cores while the GPU keeps serving.  Returns (statistics, pending checks)."""
+    import dataclasses
+
     import lesgpu
     import serve
-    if not os.path.exists(lesgpu.LIB_PATH):
-        import __graft_entry__
-        __graft_entry__.build()
-    reqs = serve.poisson_requests(args.rate, args.serve_seconds, seed=7)
+    reqs = serve.poisson_requests(rate, seconds, seed=seed)
     be = serve.GpuBackend(reserve_bytes=8 << 30)
-    check_steps = 5
-    sampled = [r.rid for r in reqs][::20][:args.check]  # every 20th request (5%), the first --check of them
-    probes = {}
+    sampled = {r.rid for r in reqs[::sample_every][:max_check]}
+    checks = []
 
-    def on_step(live):
-        for slot, (r, dom) in live.items():
-            if r.rid in sampled and r.rid not in probes:
-                n, _ = be.batch.progress(slot)
-                if n - 1 == check_steps:
-                    dom.sync()
-                    probes[r.rid] = {fid: dom.download(fid, (1, 1, 1), (r.im, r.jm, r.km))
-                                     for fid in (lesgpu.U, lesgpu.V, lesgpu.W, lesgpu.P)}
+    def on_done(r, dom):
+        if r.rid in sampled:
+            fields = {fid: dom.download(fid, (1, 1, 1), (r.im, r.jm, r.km))
+                      for fid in (lesgpu.U, lesgpu.V, lesgpu.W, lesgpu.P)}
+            checks.append(pool.apply_async(_oracle_check, ((dataclasses.asdict(be.scenario(r)), r.steps, fields),)))
 
     t_tune = time.perf_counter()
     tuned = be.pretune(reqs)  # the SOR shape of each size class, with the GPU idle
     t_tune = time.perf_counter() - t_tune
-    srv = serve.Server(be, max_live=256, setup_workers=4, on_step=on_step)
     with ClockSampler(0) as clk:
-        st = srv.run(reqs)
+        st = serve.Server(be, max_live=256, setup_workers=4, on_done=on_done).run(reqs)
     be.batch.close()
-    jobs = [(dataclasses.asdict(be.scenario(r)), check_steps, probes[r.rid]) for r in reqs if r.rid in probes]
-    errs = pool.map(_oracle_check, jobs) if jobs else []
+    st["clocks"] = clk.summary()
+    st["rate_hz"] = rate
+    st["window_s"] = seconds
+    st["sor_tuning"] = {"classes": len(tuned), "seconds": t_tune}
+    st["sampled"] = len(sampled)
+    return st, checks
+
+
+def serve_summary(st, checks):
+    errs = [c.get() for c in checks]
+    keep = ("rate_hz", "window_s", "requests", "completed", "rejected", "wall_s", "drain_s", "cell_steps_per_s",
+            "latency_s", "service_s", "queue_wait_s", "max_backlog", "mean_live_cells", "clocks")
+    out = {k: st[k] for k in keep}
+    out["oracle_check"] = {"requests": len(errs), "max_rel_err": max(errs) if errs else None, "tolerance": 1e-4,
+                           "sample": "every 20th request (5 percent); u, v, w, p at the request's final step vs the "
+                                     "FP64 oracle"}
+    return out
+
+
+def serve_lines(pool):
+    """The serving measurement carried by the headline line: the configuration's 20 req/s
+    over a shortened 8 s arrival window (the offered load, about 8e9 cell-steps/s, is
+    above what one GPU serves, so latency there is backlog), and 6 req/s over 12 s, a
+    rate the GPU sustains, for the service latency; the full 120 s window is
+    --mode serve."""
+    a = serve_window(20.0, 8.0, 7, pool)
+    b = serve_window(6.0, 12.0, 8, pool)
+    return {"at_20hz": serve_summary(*a), "sustained": serve_summary(*b),
+            "workload": "Poisson arrivals of wind scenarios, ip, jp in {64..256}, kp in {48,64,90}, 50-500 steps, "
+                        "own seed, direction and speed; admission by free HBM, continuous batching",
+            "latency": "completion latency = arrival to the end of the last step; service = admission to the end "
+                       "of the last step; queue wait = arrival to admission"}
+
+
+def run_serve(args):
+    """The serving stream alone: Poisson arrivals, admission by free HBM, continuous batching."""
+    pool = oracle_pool()
+    import lesgpu
+    if not os.path.exists(lesgpu.LIB_PATH):
+        import __graft_entry__
+        __graft_entry__.build()
+    st, checks = serve_window(args.rate, args.serve_seconds, 7, pool, max_check=args.check)
+    summ = serve_summary(st, checks)
     pool.close()
     line = {"metric": METRIC, "mode": "serve", "value": st["cell_steps_per_s"], "unit": UNIT, "n_gpus": 1,
             "higher_is_better": True, "dtype": "f32", "data": "synthetic Poisson stream of seeded urban scenarios",
             "config": {"workload": f"serving: Poisson {args.rate} req/s for {args.serve_seconds} s, grids "
                                    "ip,jp in {64..256}, kp in {48,64,90}, 50-500 steps",
-                       "rate_hz": args.rate, "window_s": args.serve_seconds},
-            "latency_s": st["latency_s"], "queue_wait_s": st["queue_wait_s"], "requests": st["requests"],
-            "completed": st["completed"], "rejected": st["rejected"], "wall_s": st["wall_s"],
-            "max_backlog": st["max_backlog"], "batch_iterations": st["batch_iterations"],
-            "mean_live_cells": st["mean_live_cells"], "clocks": clk.summary(),
-            "sor_tuning": {"classes": len(tuned), "seconds": t_tune, "before": "the arrival window"},
-            "oracle_check": {"requests": len(errs), "steps": check_steps, "max_rel_err": max(errs) if errs else None,
-                             "sample": f"every 20th request (5 percent), the first {args.check} of them; u, v, w, "
-                                       f"p after {check_steps} steps vs the FP64 oracle"}}
+                       "rate_hz": args.rate, "window_s": args.serve_seconds}}
+    line.update(summ)
     print(json.dumps(line), flush=True)
     return 0
 
@@ -611,13 +651,15 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-ensemble measurements")
     ap.add_argument("--no-parity", action="store_true", help="skip the FP64-oracle check of a short run")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement of the headline line")
     ap.add_argument("--sor-shape", default=None,
                     help="NXxNYxKCHUNK[xDEPTH]: fix the SOR tile shape (and iterations per k-march) instead of "
                          "tuning it (for runs under a profiler, whose timings would mislead the tuner)")
     ap.add_argument("--mode", default="plain", choices=["plain", "serve"])
     ap.add_argument("--serve-seconds", type=float, default=120.0, help="serve mode: arrival window")
     ap.add_argument("--rate", type=float, default=20.0, help="serve mode: requests per second")
-    ap.add_argument("--check", type=int, default=12, help="serve mode: sampled requests checked vs FP64")
+    ap.add_argument("--check", type=int, default=None,
+                    help="serve mode: check at most this many of the sampled requests vs FP64 (default: all)")
     args = ap.parse_args()
     args.dims = tuple(int(x) for x in args.dims.lower().split("x"))
     if args.warmup < 3:

@@ -207,11 +207,16 @@ class Server:
             pool.shutdown(wait=True)
         wall = clock() - t0
         lat = [done_at[r.rid] - r.arrival_s for r in requests if r.rid in done_at]
+        wait = [admitted_at[r.rid] - r.arrival_s for r in requests if r.rid in admitted_at]
+        # service time: from admission (set-up starts) to the end of the last step
+        svc = [done_at[r.rid] - admitted_at[r.rid] for r in requests if r.rid in done_at]
         work = sum(r.cells * r.steps for r in requests if r.rid in done_at)
+        last_arrival = max((r.arrival_s for r in requests), default=0.0)
         return {"requests": len(requests), "completed": len(done_at), "rejected": len(rejected), "wall_s": wall,
                 "cell_steps": work, "cell_steps_per_s": work / wall if wall > 0 else None,
                 "latency_s": {"p50": percentile(lat, 50), "p99": percentile(lat, 99), "max": max(lat) if lat else None},
-                "queue_wait_s": {"p50": percentile([admitted_at[k] - r.arrival_s for r in requests
-                                                    for k in [r.rid] if k in admitted_at], 50)},
+                "queue_wait_s": {"p50": percentile(wait, 50), "p99": percentile(wait, 99)},
+                "service_s": {"p50": percentile(svc, 50), "p99": percentile(svc, 99)},
+                "drain_s": wall - last_arrival,
                 "max_backlog": max_backlog, "batch_iterations": iters,
                 "mean_live_cells": step_cells / iters if iters else 0}

@@ -107,6 +107,12 @@ def test_server_admits_by_memory_and_completes_all(budget_cells, max_live):
     # no request completes before its own steps could have run
     assert stats["latency_s"]["p50"] > 0 and stats["latency_s"]["p99"] >= stats["latency_s"]["p50"]
     assert stats["cell_steps"] == sum(r.cells * r.steps for r in reqs)
+    # latency = queue wait + service, reported apart
+    assert 0 < stats["service_s"]["p50"] <= stats["service_s"]["p99"] <= stats["latency_s"]["max"] + 1e-9
+    assert 0 <= stats["queue_wait_s"]["p50"] <= stats["queue_wait_s"]["p99"]
+    if max_live == 4:  # slots limited: requests wait to be admitted
+        assert stats["queue_wait_s"]["p99"] > 0
+    assert stats["drain_s"] >= 0
 
 
 def test_server_batches_concurrent_requests():
