@@ -256,9 +256,21 @@ int les_batch_admit(const les_dims *dims, size_t reserve_bytes, int *ok);
 /* Add a committed handle whose next step is n0 (1 for a fresh domain), run to nmax. */
 int les_batch_add(les_batch *b, les_handle *h, int n0, int nmax, int *slot);
 int les_batch_remove(les_batch *b, int slot);  /* syncs the member first */
-/* One step of every unfinished member; *nlive = members with steps left after it. */
+/* One step of every unfinished member; *nlive = members with steps left after it.
+ * Each member's step runs up to its first SOR iteration on its own stream; SOR
+ * iterations 2..nmaxp of all members (of one tile shape) then run as one persistent
+ * launch over a work-list of every member's tiles, whose CTAs wait (bounded) for a
+ * member's previous iteration before its next; the rest of each step follows on the
+ * member's stream.  Members without a fused SOR sweep step alone. */
 int les_batch_step(les_batch *b, int *nlive);
+/* Waits for every member; fails with LES_ERR_STATE if a dependency wait of a batched
+ * SOR launch gave up since the last call (the members' SOR of that step is incomplete). */
 int les_batch_sync(les_batch *b);
+/* Bound of the batched SOR launch's dependency waits, in polls of about 128 ns (default
+ * 2^23, about a second).  hold_slot >= 0 makes that member's wait impossible, so that a
+ * test can exercise the give-up path; -1 restores normal stepping.  No counterpart in
+ * the reference. */
+int les_batch_set_wait_limit(les_batch *b, long long polls, int hold_slot);
 /* *n = the member's next step index (> nmax once finished). */
 int les_batch_slot(les_batch *b, int slot, int *n, int *nmax);
 int les_batch_last_error(les_batch *b, char *buf, size_t len);

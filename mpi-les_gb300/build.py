@@ -27,7 +27,7 @@ NVCC_FLAGS = ARCH + [
 ]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall"]
 
-CU_SOURCES = ["les_kernels.cu", "les_fused.cu", "les_sor.cu", "les_sor16.cu", "les_sor2.cu", "les_step.cu", "les_api.cu", "les_noalloc.cu", "les_batch.cu", "les_tune.cu", "les_aveflow.cu"]
+CU_SOURCES = ["les_kernels.cu", "les_fused.cu", "les_sor.cu", "les_sor16.cu", "les_sor2.cu", "les_sor_batch.cu", "les_step.cu", "les_api.cu", "les_noalloc.cu", "les_batch.cu", "les_tune.cu", "les_aveflow.cu"]
 CXX_SOURCES = ["setup.cpp", "les_io.cpp"]
 
 

@@ -18,6 +18,7 @@
 #include "les_aveflow.cuh"
 #include "les_common.cuh"
 #include "les_kernels.cuh"
+#include "les_sor_batch.cuh"
 #include "les_step.cuh"
 #include "les_tune.cuh"
 
@@ -887,6 +888,33 @@ extern "C" int les_gpu_step(les_handle *h, int n, int nmax) {
   if (rc) return fail(h, LES_ERR_CUDA, std::string("step: ") + cudaGetErrorString(cudaGetLastError()));
   return check_launch(h, "step");
 }
+
+// ---- for les_batch.cu: a member's view for a batched SOR launch, and its step parts
+// *ok = 1 when the member's SOR iterations 2..nmaxp can run in a batched launch: a
+// committed domain, p consistent with its halos, a fused-sweep plan whose tensor maps
+// fit the one-iteration TMA sweep.
+int les_handle_batch_view(les_handle *h, const LesDom **d, SorShape *sh, const LesSorMaps **maps, int *nmaxp,
+                          cudaStream_t *s, int *ok) {
+  *ok = 0;
+  if (!h || !h->committed) return LES_OK;
+  *s = h->s;
+  if (h->p_dirty) return LES_OK;
+  const SorShape plan = les_step_plan_shape(h->dom, &h->plan);
+  if (plan.ny <= 0 || !les_sor_batch_ok(h->dom, plan, &h->plan.maps)) return LES_OK;
+  *d = &h->dom;
+  *sh = SorShape{plan.nx, plan.ny, h->dom.km, 1};
+  *maps = &h->plan.maps;
+  *nmaxp = h->prm.nmaxp;
+  *ok = 1;
+  return LES_OK;
+}
+int les_handle_step_part(les_handle *h, int n, int part) {
+  NEED_COMMIT(h);
+  const int rc = les_step_run_part(h->dom, h->prm, &h->plan, n, part, ctx_of(h));
+  if (rc) return fail(h, LES_ERR_CUDA, std::string("step part: ") + cudaGetErrorString(cudaGetLastError()));
+  return check_launch(h, "step part");
+}
+void les_handle_count_launches(les_handle *h, long long k) { h->nlaunch += k; }
 
 extern "C" int les_gpu_run(les_handle *h, int n0, int nsteps, int nmax) {
   NEED_COMMIT(h);

@@ -2,13 +2,20 @@
 // continuous batching of the serving loop.
 //
 // A batch holds domain handles (each with its own device state, CUDA stream and
-// captured step graph) and a per-slot step counter.  les_batch_step enqueues one time
-// step of every live member -- each member's graph on its own stream, no host
-// synchronisation -- so the members' kernels overlap on the GPU: a 150x150x90 domain
-// fills only a fraction of the 152 SMs per kernel, many of them fill it.  Members join
-// and leave between steps (continuous batching); nothing in a member's arithmetic
-// depends on the others, so a domain's result is the same alone and in any mix.
-// Calls on one batch are serialised by its mutex.
+// captured step graphs) and a per-slot step counter.  les_batch_step enqueues one time
+// step of every live member without host synchronisation:
+//   1. each member's step up to its first SOR iteration (a captured graph on the
+//      member's stream; the members' kernels overlap on the GPU);
+//   2. SOR iterations 2..nmaxp of all members at once: one persistent launch per tile
+//      shape over a work-list of every member's tiles (les_sor_batch.cu), on a stream of
+//      the batch that waits for step 1 of its members;
+//   3. each member's copy-out, pav and boundary conditions (a captured graph on the
+//      member's stream, after the batched launch).
+// A member whose SOR cannot take part (no fused sweep: odd jm, km too large; a state
+// just uploaded) steps through its own whole-step graph.  Members join and leave
+// between steps (continuous batching); nothing in a member's arithmetic depends on the
+// others, so a domain's result is the same alone and in any mix, bit for bit.  Calls on
+// one batch are serialised by its mutex.
 //
 // Concurrency across streams is limited by CUDA_DEVICE_MAX_CONNECTIONS (8 unless the
 // process sets it, before CUDA initialises, up to 32).  Members share the GPU, so
@@ -17,22 +24,44 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <map>
 #include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "../../include/les_gpu.h"
+#include "les_sor_batch.cuh"
 
-// les_api.cu: stop splitting the member's SOR march (the GPU is shared)
+// les_api.cu: stop splitting the member's SOR march (the GPU is shared); the member's
+// view for a batched SOR launch; its step parts around the batched iterations
 void les_handle_share_gpu(les_handle *h);
+int les_handle_batch_view(les_handle *h, const LesDom **d, SorShape *sh, const LesSorMaps **maps, int *nmaxp,
+                          cudaStream_t *s, int *ok);
+int les_handle_step_part(les_handle *h, int n, int part);
 
 struct les_batch {
   struct Slot {
     les_handle *h = nullptr;
     int n = 0, nmax = 0;  // next step index; the member is finished once n > nmax
     bool used = false;
+    cudaEvent_t ev = nullptr;  // end of the member's part 1 in this step
+  };
+  // one batched SOR launch: the members of one tile shape and iteration count
+  struct Group {
+    SorShape sh;
+    int nmaxp = 0;
+    std::vector<int> slots;
+    SorBatchBuffers buf;
+    cudaStream_t s = nullptr;
+    cudaEvent_t done = nullptr;
   };
   std::vector<Slot> slots;
+  std::vector<Group> groups;
+  std::vector<std::tuple<int, les_handle *, int, int, int>> key;  // (slot, handle, nx, ny, nmaxp) of the groups
+  long long spin_limit = 1LL << 23;  // polls (about 128 ns each) before a dependency wait gives up
+  int hold_slot = -1;                // test hook: this member's wait can never end
+  int sms = 0;
   std::mutex mu;
   std::string err;
 };
@@ -56,6 +85,14 @@ extern "C" int les_batch_destroy(les_batch *b) {
     std::lock_guard<std::mutex> lock(b->mu);
     for (auto &s : b->slots)
       if (s.used && s.h) les_gpu_sync(s.h);
+    for (auto &g : b->groups) {
+      if (g.s) cudaStreamSynchronize(g.s);
+      les_sor_batch_free(&g.buf);
+      if (g.s) cudaStreamDestroy(g.s);
+      if (g.done) cudaEventDestroy(g.done);
+    }
+    for (auto &s : b->slots)
+      if (s.ev) cudaEventDestroy(s.ev);
   }
   delete b;
   return LES_OK;
@@ -99,27 +136,136 @@ extern "C" int les_batch_remove(les_batch *b, int slot) {
   if (slot < 0 || slot >= (int)b->slots.size() || !b->slots[slot].used)
     return bfail(b, LES_ERR_ARG, "batch_remove: no such slot");
   les_gpu_sync(b->slots[slot].h);
+  cudaEvent_t ev = b->slots[slot].ev;
   b->slots[slot] = les_batch::Slot();
+  b->slots[slot].ev = ev;
   return LES_OK;
 }
+
+namespace {
+
+// Regroup the batched members when the membership (or a member's shape) changed: waits
+// for the groups' launches in flight, then uploads the new work lists.
+int regroup(les_batch *b, const std::vector<std::tuple<int, les_handle *, int, int, int>> &key,
+            const std::vector<const LesDom *> &doms, const std::vector<const LesSorMaps *> &maps) {
+  if (key == b->key) return LES_OK;
+  for (auto &g : b->groups)
+    if (g.s && cudaStreamSynchronize(g.s) != cudaSuccess) return LES_ERR_CUDA;
+  std::map<std::tuple<int, int, int>, std::vector<int>> by;  // (nx, ny, nmaxp) -> indices into key
+  for (int q = 0; q < (int)key.size(); ++q) by[{std::get<2>(key[q]), std::get<3>(key[q]), std::get<4>(key[q])}].push_back(q);
+  // reuse the existing groups' buffers and streams where they exist
+  while (b->groups.size() < by.size()) b->groups.emplace_back();
+  size_t gi = 0;
+  for (auto &kv : by) {
+    les_batch::Group &g = b->groups[gi++];
+    if (!g.s && cudaStreamCreateWithFlags(&g.s, cudaStreamNonBlocking) != cudaSuccess) return LES_ERR_CUDA;
+    if (!g.done && cudaEventCreateWithFlags(&g.done, cudaEventDisableTiming) != cudaSuccess) return LES_ERR_CUDA;
+    g.sh = SorShape{std::get<0>(kv.first), std::get<1>(kv.first), 0, 1};
+    g.nmaxp = std::get<2>(kv.first);
+    g.slots.clear();
+    std::vector<const LesDom *> gd;
+    std::vector<const LesSorMaps *> gm;
+    for (int q : kv.second) {
+      g.slots.push_back(std::get<0>(key[q]));
+      gd.push_back(doms[q]);
+      gm.push_back(maps[q]);
+    }
+    if (les_sor_batch_prepare(gd, gm, g.sh, g.nmaxp, &g.buf) != 0) return LES_ERR_NOMEM;
+  }
+  for (size_t q = gi; q < b->groups.size(); ++q) b->groups[q].slots.clear();  // unused now
+  b->key = key;
+  return LES_OK;
+}
+
+}  // namespace
 
 extern "C" int les_batch_step(les_batch *b, int *nlive) {
   if (!b) return LES_ERR_ARG;
   std::lock_guard<std::mutex> lock(b->mu);
-  int live = 0;
+  if (!b->sms) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+      (void)cudaGetLastError();
+      b->sms = 152;
+    }
+  }
+  auto member_fail = [&](int q, int rc, const char *what) {
+    char m[256];
+    les_gpu_last_error(b->slots[q].h, m, sizeof m);
+    return bfail(b, rc, std::string("batch_step: slot ") + std::to_string(q) + " " + what + ": " + m);
+  };
+  // the live members, and which of them take part in the batched SOR launches
+  std::vector<std::tuple<int, les_handle *, int, int, int>> key;
+  std::vector<const LesDom *> doms;
+  std::vector<const LesSorMaps *> maps;
+  std::vector<int> alone;
+  std::vector<cudaStream_t> streams(b->slots.size(), nullptr);
   for (int q = 0; q < (int)b->slots.size(); ++q) {
     auto &s = b->slots[q];
     if (!s.used || s.n > s.nmax) continue;
-    const int rc = les_gpu_step(s.h, s.n, s.nmax);
-    if (rc) {
-      char m[256];
-      les_gpu_last_error(s.h, m, sizeof m);
-      return bfail(b, rc, "batch_step: slot " + std::to_string(q) + ": " + m);
+    const LesDom *d = nullptr;
+    SorShape sh;
+    const LesSorMaps *mp = nullptr;
+    int nmaxp = 0, ok = 0;
+    les_handle_batch_view(s.h, &d, &sh, &mp, &nmaxp, &streams[q], &ok);
+    if (!ok || nmaxp < 2) {
+      alone.push_back(q);
+      continue;
     }
+    key.emplace_back(q, s.h, sh.nx, sh.ny, nmaxp);
+    doms.push_back(d);
+    maps.push_back(mp);
+  }
+  int rc = regroup(b, key, doms, maps);
+  if (rc) return bfail(b, rc, "batch_step: building the batched SOR work list failed");
+  // 1. each batched member up to its first SOR iteration, on its own stream
+  for (const auto &g : b->groups)
+    for (int q : g.slots) {
+      auto &s = b->slots[q];
+      if ((rc = les_handle_step_part(s.h, s.n, 1))) return member_fail(q, rc, "part 1");
+      if (!s.ev && cudaEventCreateWithFlags(&s.ev, cudaEventDisableTiming) != cudaSuccess)
+        return bfail(b, LES_ERR_CUDA, "batch_step: event");
+      if (cudaEventRecord(s.ev, streams[q]) != cudaSuccess) return bfail(b, LES_ERR_CUDA, "batch_step: event record");
+    }
+  // 2. SOR iterations 2..nmaxp of each group's members in one persistent launch
+  for (auto &g : b->groups) {
+    if (g.slots.empty()) continue;
+    for (int q : g.slots)
+      if (cudaStreamWaitEvent(g.s, b->slots[q].ev, 0) != cudaSuccess) return bfail(b, LES_ERR_CUDA, "batch_step: wait");
+    int hold = -1;
+    for (int m = 0; m < (int)g.slots.size(); ++m)
+      if (g.slots[m] == b->hold_slot) hold = m;
+    if (les_sor_batch_launch(g.buf, b->sms, b->spin_limit, hold, g.s) != 0)
+      return bfail(b, LES_ERR_CUDA, std::string("batch_step: batched SOR launch: ") + cudaGetErrorString(cudaGetLastError()));
+    if (cudaEventRecord(g.done, g.s) != cudaSuccess) return bfail(b, LES_ERR_CUDA, "batch_step: event record");
+  }
+  // 3. each batched member's copy-out, pav and boundary conditions, after its group
+  for (const auto &g : b->groups)
+    for (int q : g.slots) {
+      if (cudaStreamWaitEvent(streams[q], g.done, 0) != cudaSuccess) return bfail(b, LES_ERR_CUDA, "batch_step: wait");
+      if ((rc = les_handle_step_part(b->slots[q].h, b->slots[q].n, 2))) return member_fail(q, rc, "part 2");
+    }
+  // members outside the batched launches: their whole step
+  for (int q : alone) {
+    auto &s = b->slots[q];
+    if ((rc = les_gpu_step(s.h, s.n, s.nmax))) return member_fail(q, rc, "step");
+  }
+  int live = 0;
+  for (auto &s : b->slots) {
+    if (!s.used || s.n > s.nmax) continue;
     ++s.n;
     if (s.n <= s.nmax) ++live;
   }
   if (nlive) *nlive = live;
+  return LES_OK;
+}
+
+extern "C" int les_batch_set_wait_limit(les_batch *b, long long polls, int hold_slot) {
+  if (!b || polls < 1) return LES_ERR_ARG;
+  std::lock_guard<std::mutex> lock(b->mu);
+  b->spin_limit = polls;
+  b->hold_slot = hold_slot;
   return LES_OK;
 }
 
@@ -131,6 +277,19 @@ extern "C" int les_batch_sync(les_batch *b) {
     if (!s.used) continue;
     const int rc = les_gpu_sync(s.h);
     if (rc) return bfail(b, rc, "batch_sync: slot " + std::to_string(q));
+  }
+  for (auto &g : b->groups) {
+    if (!g.s) continue;
+    int st = 0;
+    if (les_sor_batch_status(g.buf, g.s, &st) != 0) return bfail(b, LES_ERR_CUDA, "batch_sync: batched SOR");
+    if (st) {
+      // clear the record, so that later steps report only their own failures
+      if (g.buf.counters) cudaMemsetAsync(g.buf.counters + 1, 0, sizeof(unsigned), g.s);
+      cudaStreamSynchronize(g.s);
+      return bfail(b, LES_ERR_STATE,
+                   "batch_sync: a dependency wait of the batched SOR launch gave up; the members' SOR of that step "
+                   "did not finish (their CT_ERROR word is set)");
+    }
   }
   return LES_OK;
 }

@@ -110,16 +110,17 @@ struct Lane {
   unsigned gmask;  // ghost rows that copy row jr (ghost_mask)
 };
 
+// bx, by: the tile's column and row in the domain's tile grid
 template <int NX>
-__device__ __forceinline__ Lane make_lane(const LesDom &d, int tj, int ny) {
+__device__ __forceinline__ Lane make_lane(const LesDom &d, int tj, int ny, int bx, int by) {
   Lane L;
   L.c4 = threadIdx.x;
   // 16-column tiles: a warp holds two rows two apart (rows 0,2 | 1,3 | 4,6 | 5,7 ...), so
   // both rows have the same red/black parity and the colour branch stays warp-uniform
   L.r = (NX == 16) ? 4 * ((int)threadIdx.y >> 2) + (((int)threadIdx.y >> 1) & 1) + 2 * ((int)threadIdx.y & 1)
                    : (int)threadIdx.y;
-  const int i0 = 1 + blockIdx.x * tile_i(NX);
-  const int j0 = 1 + blockIdx.y * tj;
+  const int i0 = 1 + bx * tile_i(NX);
+  const int j0 = 1 + by * tj;
   L.ib = i0 - 4 + 4 * L.c4;
   L.jr = j0 - 2 + L.r;
   int jw = (L.jr - 1) % d.jm;
@@ -157,16 +158,16 @@ __device__ __forceinline__ void store_final(const LesDom &d, const SorArgs &a, c
 
 // FP32 (Kahan) per thread -> FP64 per CTA -> last CTA sums the CTA partials in order.
 // warp[] holds one double per warp of the CTA (NX * NY / 32).
+// cta: the CTA's index among the a.ntiles partials of this iteration
 template <int NX, int NY>
 __device__ __forceinline__ void finish_residual(const LesDom &d, const SorArgs &a, float acc, double *warp,
-                                                int *last) {
+                                                int *last, int cta) {
   constexpr int NW = NX * NY / 32;
   const int tid = threadIdx.y * NX + threadIdx.x, lane = tid & 31, wid = tid >> 5;
   float x = acc;
   for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
   if (lane == 0) warp[wid] = (double)x;
   __syncthreads();
-  const int cta = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
   if (tid == 0) {
     double t = 0.0;
     for (int q = 0; q < NW; ++q) t += warp[q];
@@ -226,7 +227,7 @@ __global__ void __launch_bounds__(NX *NY, min_ctas(NX)) k_sor_reg(LesDom d, SorA
   // must be cut back to its first iteration
   if (a.redo ? d.ctl[CT_REDO] == 0 : d.ctl[CT_CONVERGED] != 0) return;
 
-  const Lane L = make_lane<NX>(d, a.tj, NY);
+  const Lane L = make_lane<NX>(d, a.tj, NY, blockIdx.x, blockIdx.y);
   const int c4 = L.c4, r = L.r, ib = L.ib, jw = L.jw;
   const int im = d.im, jm = d.jm, km = d.km;
   const bool col_load = (ib <= im + 1);
@@ -393,7 +394,7 @@ __global__ void __launch_bounds__(NX *NY, min_ctas(NX)) k_sor_reg(LesDom d, SorA
     if (s0 + 5 > s_end) break;
     step(IC<5>{}, s0 + 5);
   }
-  finish_residual<NX, NY>(d, a, acc, sWarp, &sLast);
+  finish_residual<NX, NY>(d, a, acc, sWarp, &sLast, (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x);
 }
 
 // ---------------------------------------------------------------------------------
@@ -448,16 +449,15 @@ struct TmaSmem {
   int last, abort_;
 };
 
+// One tile of one iteration: tile (bx, by) of the domain's tile grid, k chunk bz, partial
+// slot cta; tmP / tmR: tensor maps of the source p buffer and of rhs (kernel parameters
+// or global memory).  Every thread of the CTA calls it; it leaves the mbarriers
+// quiescent (every copy it issued has been waited for).
 template <int NX, int NY, int D, bool KC>
-__global__ void __launch_bounds__(NX *NY, min_ctas(NX))
-    k_sor_tma(LesDom d, SorArgs a, const __grid_constant__ CUtensorMap tmP, const __grid_constant__ CUtensorMap tmR) {
-  extern __shared__ __align__(1024) unsigned char smem_raw[];
-  TmaSmem<NX, NY, D> &S = *reinterpret_cast<TmaSmem<NX, NY, D> *>(smem_raw);
-  // early exit of press.f95:119-121; in redo mode: run only when a two-iteration launch
-  // must be cut back to its first iteration
-  if (a.redo ? d.ctl[CT_REDO] == 0 : d.ctl[CT_CONVERGED] != 0) return;
-
-  const Lane L = make_lane<NX>(d, a.tj, NY);
+__device__ __forceinline__ void sor_tma_tile(const LesDom &d, const SorArgs &a, const CUtensorMap *tmP,
+                                             const CUtensorMap *tmR, int bx, int by, int bz, int cta,
+                                             TmaSmem<NX, NY, D> &S) {
+  const Lane L = make_lane<NX>(d, a.tj, NY, bx, by);
   const int c4 = L.c4, r = L.r, ib = L.ib, jw = L.jw;
   const int km = d.km;
   float c2l[4], c2s[4];
@@ -471,12 +471,12 @@ __global__ void __launch_bounds__(NX *NY, min_ctas(NX))
   // omega = 1 (press.f95:45, the only value this kernel is launched for): omega * x is x
   constexpr float omega = 1.f;
   const bool producer = (r == 0) && (c4 == 0);
-  const int tx = blockIdx.x * tile_i(NX);  // padded column of i0 - 4
-  const int ty = blockIdx.y * a.tj + (LES_JOFF - 1);  // padded row of j0 - 2
+  const int tx = bx * tile_i(NX);               // padded column of i0 - 4
+  const int ty = by * a.tj + (LES_JOFF - 1);     // padded row of j0 - 2
   const uint32_t stage_bytes = 2u * NY * NX * 16u;
   // this CTA's k chunk [ka, kb], marched from ka-1 (a red ring plane) to kb+1; it
   // loads planes mfirst .. mlast, plane m into stage (m - mfirst) % D
-  const int ka = KC ? 1 + (int)blockIdx.z * a.kchunk : 1;
+  const int ka = KC ? 1 + bz * a.kchunk : 1;
   const int kb = KC ? min(km, ka + a.kchunk - 1) : km;
   const int s_begin = KC ? max(1, ka - 1) : 1;
   const int s_end = KC ? min(km + 1, kb + 1) : km + 1;
@@ -485,8 +485,8 @@ __global__ void __launch_bounds__(NX *NY, min_ctas(NX))
   auto issue = [&](int m) {  // plane m (mfirst..mlast) into stage (m - mfirst) % D
     const int q = (m - mfirst) % D;
     mbar_expect_tx(&S.bar[q], stage_bytes);
-    tma_load_3d(&S.p[q][0][0], &tmP, tx, ty, m + LES_KOFF, &S.bar[q]);
-    tma_load_3d(&S.rhs[q][0][0], &tmR, tx, ty, m + LES_KOFF, &S.bar[q]);
+    tma_load_3d(&S.p[q][0][0], tmP, tx, ty, m + LES_KOFF, &S.bar[q]);
+    tma_load_3d(&S.rhs[q][0][0], tmR, tx, ty, m + LES_KOFF, &S.bar[q]);
   };
 
   if (producer) {
@@ -632,7 +632,19 @@ __global__ void __launch_bounds__(NX *NY, min_ctas(NX))
     for (int m = failed_at; m <= mlast && m < failed_at + D; ++m)
       (void)mbar_wait(&S.bar[(m - mfirst) % D], (uint32_t)(((m - mfirst) / D) & 1));
   }
-  finish_residual<NX, NY>(d, a, acc, S.warp, &S.last);
+  finish_residual<NX, NY>(d, a, acc, S.warp, &S.last, cta);
+}
+
+template <int NX, int NY, int D, bool KC>
+__global__ void __launch_bounds__(NX *NY, min_ctas(NX))
+    k_sor_tma(LesDom d, SorArgs a, const __grid_constant__ CUtensorMap tmP, const __grid_constant__ CUtensorMap tmR) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  TmaSmem<NX, NY, D> &S = *reinterpret_cast<TmaSmem<NX, NY, D> *>(smem_raw);
+  // early exit of press.f95:119-121; in redo mode: run only when a two-iteration launch
+  // must be cut back to its first iteration
+  if (a.redo ? d.ctl[CT_REDO] == 0 : d.ctl[CT_CONVERGED] != 0) return;
+  sor_tma_tile<NX, NY, D, KC>(d, a, &tmP, &tmR, blockIdx.x, blockIdx.y, blockIdx.z,
+                              (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x, S);
 }
 
 template <int NX, int NY, bool KC>

@@ -37,6 +37,11 @@ void les_step_plan_free(LesStepPlan *plan) {
     plan->exec[q] = nullptr;
     plan->launches[q] = 0;
   }
+  for (int q = 0; q < 3; ++q) {
+    if (plan->part_exec[q]) cudaGraphExecDestroy(plan->part_exec[q]);
+    plan->part_exec[q] = nullptr;
+    plan->part_launches[q] = 0;
+  }
   plan->sor = SorShape{};
   plan->sor_picked = 0;
   plan->maps.valid = 0;
@@ -176,6 +181,72 @@ void les_step_enqueue(const LesDom &d, const les_params &prm, SorShape sh, const
     les_launch_sor_simple(d, prm.nmaxp, ctx);
   }
   les_launch_pav_adjust(d, ctx);
+}
+
+// Part 1: the step up to SOR iteration 1; part 2: after the last SOR iteration.
+static void enqueue_part(const LesDom &d, const les_params &prm, SorShape sh, const LesSorMaps *maps, int n, int part,
+                         LesCtx ctx) {
+  if (part == 1) {
+    les_launch_velnw(d, ctx);
+    les_launch_bondv1(d, n, ctx);
+    les_launch_velfg_fused(d, true, ctx);  // velfg + feedbf
+    les_launch_les_fused(d, true, ctx);    // les + adam
+    les_launch_bondfg(d, ctx);
+    les_launch_rhs_sor(d, ctx);
+    les_launch_sor_begin(d, ctx);
+    SorShape one = sh;
+    one.depth = 1;
+    const int kchunk = one.kchunk > 0 ? one.kchunk : d.km;
+    const int nchunk = (d.km + kchunk - 1) / kchunk;
+    SorArgs a;
+    a.psrc = d.p;
+    a.pdst = d.sorB;  // iteration 1 always leaves p for the batched iterations (or the copy-out)
+    a.dstcode = 1;
+    a.ghost = 1;
+    a.rhs = d.sorR;
+    a.depth = 1;
+    a.tj = one.ny - 4;
+    a.kchunk = kchunk;
+    a.nchunk = nchunk;
+    a.ntiles = les_sor_fused_tiles(d.im, d.jm, one) * nchunk;
+    a.part = d.part;
+    a.counter = d.cnt;
+    les_launch_sor_iter(d, a, one, nullptr, ctx.s);  // reads p: the register kernel
+    ++*ctx.nlaunch;
+    (void)maps;
+    (void)prm;
+  } else {
+    les_launch_sor_copyout(d, prm.nmaxp, ctx.s);
+    ++*ctx.nlaunch;
+    les_launch_pav_adjust(d, ctx);
+  }
+}
+
+int les_step_run_part(const LesDom &d, const les_params &prm, LesStepPlan *plan, int n, int part, LesCtx ctx) {
+  plan_pick(d, plan);
+  if (plan->sor.ny <= 0) return (int)cudaErrorInvalidValue;
+  const int q = (part == 2) ? 2 : ((n == 1) ? 0 : 1);
+  if (!plan->part_exec[q]) {
+    cudaGraph_t g = nullptr;
+    long long cnt = 0;
+    LesCtx cap{ctx.s, &cnt};
+    cudaError_t e = cudaStreamBeginCapture(ctx.s, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return (int)e;
+    enqueue_part(d, prm, plan->sor, &plan->maps, n, part, cap);
+    e = cudaStreamEndCapture(ctx.s, &g);
+    if (e != cudaSuccess) return (int)e;
+    e = cudaGraphInstantiate(&plan->part_exec[q], g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      plan->part_exec[q] = nullptr;
+      return (int)e;
+    }
+    plan->part_launches[q] = cnt;
+  }
+  cudaError_t e = cudaGraphLaunch(plan->part_exec[q], ctx.s);
+  if (e != cudaSuccess) return (int)e;
+  *ctx.nlaunch += plan->part_launches[q];
+  return 0;
 }
 
 int les_step_run(const LesDom &d, const les_params &prm, LesStepPlan *plan, int n, int nmax, LesCtx ctx) {

@@ -11,6 +11,10 @@
 struct LesStepPlan {
   cudaGraphExec_t exec[2] = {nullptr, nullptr};
   long long launches[2] = {0, 0};  // kernels inside each graph
+  // the step cut around SOR iterations 2..nmaxp, for batches whose SOR runs in one
+  // persistent launch over all members: [0] before (n == 1), [1] before (n > 1), [2] after
+  cudaGraphExec_t part_exec[3] = {nullptr, nullptr, nullptr};
+  long long part_launches[3] = {0, 0, 0};
   SorShape sor;                    // fused SOR tile shape (sor.ny == 0: per-subroutine path)
   int sor_picked = 0;              // sor chosen (and maps made) for this plan
   LesSorMaps maps;                 // tensor maps of the SOR buffers for sor
@@ -37,3 +41,8 @@ void les_step_velfg_pass(const LesDom &d, LesCtx ctx);
 void les_step_les_pass(const LesDom &d, LesCtx ctx);
 // The launch sequence itself (no graph), used for capture and by tests.
 void les_step_enqueue(const LesDom &d, const les_params &prm, SorShape sh, const LesSorMaps *maps, int n, LesCtx ctx);
+// The step in two parts around SOR iterations 2..nmaxp (which a batched launch runs,
+// les_sor_batch.cu): part 1 is velnw .. rhs and SOR iteration 1 (p into sorB), part 2
+// the copy-out of the last SOR result, pav and the final boundary conditions.  Needs a
+// plan with a fused sweep.  Returns 0 or a CUDA error code.
+int les_step_run_part(const LesDom &d, const les_params &prm, LesStepPlan *plan, int n, int part, LesCtx ctx);

@@ -219,6 +219,7 @@ def load_library(path: str | None = None) -> C.CDLL:
         "les_batch_step": (C.c_int, [vp, ip_]),
         "les_batch_sync": (C.c_int, [vp]),
         "les_batch_slot": (C.c_int, [vp, C.c_int, ip_, ip_]),
+        "les_batch_set_wait_limit": (C.c_int, [vp, C.c_longlong, C.c_int]),
         "les_batch_last_error": (C.c_int, [vp, C.c_char_p, C.c_size_t]),
     }
     for name, (res, args) in sig.items():
@@ -551,8 +552,9 @@ class Domain:
 
 
 class Batch:
-    """Many resident domains stepped together (les_batch_*): each member's step graph on
-    its own stream, members joining and leaving between steps."""
+    """Many resident domains stepped together (les_batch_*): each member's step on its own
+    stream around one persistent SOR launch over all members' tiles, members joining and
+    leaving between steps."""
 
     def __init__(self):
         self.lib = load_library()
@@ -596,6 +598,11 @@ class Batch:
 
     def sync(self):
         self._check(self.lib.les_batch_sync(self._b), "sync")
+
+    def set_wait_limit(self, polls: int, hold_slot: int = -1) -> None:
+        """Bound the batched SOR launch's dependency waits (polls of about 128 ns); a
+        hold_slot >= 0 makes that member's wait impossible (the give-up path, for tests)."""
+        self._check(self.lib.les_batch_set_wait_limit(self._b, polls, hold_slot), "set_wait_limit")
 
     def progress(self, slot: int) -> tuple[int, int]:
         """(next step index, nmax) of a member; finished once next > nmax."""

@@ -113,3 +113,73 @@ def test_serving_small_stream_matches_alone(built_lib):
             y = alone.download(fid)
             assert np.array_equal(x.view(np.uint32), y.view(np.uint32)), (r.rid, lesgpu.FIELD_NAMES[fid])
     be.batch.close()
+
+
+def test_batched_sor_groups_and_fallbacks_match_alone(built_lib):
+    """Members of two tile shapes (two batched SOR launches), a member whose SOR cannot
+    be batched (odd jm: the per-subroutine sweep) and a member at its first step, all in
+    one batch: each ends bitwise equal to the same domain stepped alone, and a batched
+    member issues fewer launches of its own than its whole-step graph would."""
+    params = lesgpu.Params(nmaxp=12)
+    specs = [(scenario(150, 60, 14, seed=301, direction_deg=10.0), (32, 24, 0, 1)),
+             (scenario(120, 48, 12, seed=302, direction_deg=140.0), (16, 20, 0, 1)),
+             (scenario(96, 40, 10, seed=303, direction_deg=250.0), (32, 20, 0, 1)),
+             (scenario(40, 21, 9, seed=304), None)]
+    alone = []
+    for sc, shape in specs:
+        d = make_gpu(sc, params)
+        if shape:
+            d.set_sor_shape(*shape)
+        for n in range(1, 6):
+            d.step(n, 5)
+        d.sync()
+        alone.append(d)
+    b = lesgpu.Batch()
+    doms = []
+    for sc, shape in specs:
+        d = make_gpu(sc, params)
+        if shape:
+            d.set_sor_shape(*shape)
+        doms.append(d)
+        b.add(d, 1, 5)
+    l0 = doms[0].launch_count()
+    while b.step() > 0:
+        pass
+    b.sync()
+    per_step = (doms[0].launch_count() - l0) / 5
+    for q, (x, y) in enumerate(zip(doms, alone)):
+        _same(x, y, f"member {q}")
+    whole = make_gpu(specs[0][0], params)
+    whole.set_sor_shape(*specs[0][1])
+    whole.step(1, 5)
+    w0 = whole.launch_count()
+    whole.step(2, 5)
+    assert per_step < (whole.launch_count() - w0) - params.nmaxp + 5, per_step
+    b.close()
+
+
+def test_batched_sor_wait_gives_up_and_reports(built_lib):
+    """A dependency wait of the persistent SOR launch that can never end (a member held
+    on a count nothing reaches) gives up after its bound, the launch stops, and
+    les_batch_sync reports it; the GPU stays usable and the next batch steps normally."""
+    params = lesgpu.Params(nmaxp=6)
+    b = lesgpu.Batch()
+    doms = [make_gpu(scenario(64, 40, 12, seed=311 + q), params) for q in range(2)]
+    slots = [b.add(d, 1, 3) for d in doms]
+    b.set_wait_limit(1 << 14, hold_slot=slots[0])  # about 2 ms of polling
+    b.step()
+    with pytest.raises(lesgpu.LesError, match="gave up"):
+        b.sync()
+    b.set_wait_limit(1 << 23, hold_slot=-1)
+    b.close()
+    # a fresh batch on the same GPU: steps and matches the domain alone
+    sc = scenario(64, 40, 12, seed=321)
+    ref = _alone(sc, params, 3)
+    b2 = lesgpu.Batch()
+    d = make_gpu(sc, params)
+    b2.add(d, 1, 3)
+    while b2.step() > 0:
+        pass
+    b2.sync()
+    _same(d, ref, "after a failed wait")
+    b2.close()
