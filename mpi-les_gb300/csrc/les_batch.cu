@@ -144,35 +144,52 @@ extern "C" int les_batch_remove(les_batch *b, int slot) {
 
 namespace {
 
-// Regroup the batched members when the membership (or a member's shape) changed: waits
-// for the groups' launches in flight, then uploads the new work lists.
+// Group the batched members by (tile shape, iteration count) and bring each group's
+// member table and work list up to date.  Tables are compared by content (a handle freed
+// and another created at the same address is a different member); when any differs,
+// the launches in flight finish before the new tables are uploaded.
 int regroup(les_batch *b, const std::vector<std::tuple<int, les_handle *, int, int, int>> &key,
             const std::vector<const LesDom *> &doms, const std::vector<const LesSorMaps *> &maps) {
-  if (key == b->key) return LES_OK;
-  for (auto &g : b->groups)
-    if (g.s && cudaStreamSynchronize(g.s) != cudaSuccess) return LES_ERR_CUDA;
   std::map<std::tuple<int, int, int>, std::vector<int>> by;  // (nx, ny, nmaxp) -> indices into key
   for (int q = 0; q < (int)key.size(); ++q) by[{std::get<2>(key[q]), std::get<3>(key[q]), std::get<4>(key[q])}].push_back(q);
-  // reuse the existing groups' buffers and streams where they exist
   while (b->groups.size() < by.size()) b->groups.emplace_back();
+  struct Pending {
+    size_t g;
+    std::vector<SorBatchDom> host;
+    std::vector<int> owner;
+  };
+  std::vector<Pending> changed;
   size_t gi = 0;
   for (auto &kv : by) {
-    les_batch::Group &g = b->groups[gi++];
+    les_batch::Group &g = b->groups[gi];
     if (!g.s && cudaStreamCreateWithFlags(&g.s, cudaStreamNonBlocking) != cudaSuccess) return LES_ERR_CUDA;
     if (!g.done && cudaEventCreateWithFlags(&g.done, cudaEventDisableTiming) != cudaSuccess) return LES_ERR_CUDA;
-    g.sh = SorShape{std::get<0>(kv.first), std::get<1>(kv.first), 0, 1};
-    g.nmaxp = std::get<2>(kv.first);
-    g.slots.clear();
+    const SorShape sh{std::get<0>(kv.first), std::get<1>(kv.first), 0, 1};
+    const int nmaxp = std::get<2>(kv.first);
     std::vector<const LesDom *> gd;
     std::vector<const LesSorMaps *> gm;
+    std::vector<int> slots;
     for (int q : kv.second) {
-      g.slots.push_back(std::get<0>(key[q]));
+      slots.push_back(std::get<0>(key[q]));
       gd.push_back(doms[q]);
       gm.push_back(maps[q]);
     }
-    if (les_sor_batch_prepare(gd, gm, g.sh, g.nmaxp, &g.buf) != 0) return LES_ERR_NOMEM;
+    Pending p{gi, {}, {}};
+    if (les_sor_batch_build(gd, gm, sh, nmaxp, g.buf, &p.host, &p.owner)) changed.push_back(std::move(p));
+    g.sh = sh;
+    g.nmaxp = nmaxp;
+    g.slots = slots;
+    ++gi;
   }
   for (size_t q = gi; q < b->groups.size(); ++q) b->groups[q].slots.clear();  // unused now
+  if (!changed.empty()) {
+    for (auto &g : b->groups)
+      if (g.s && cudaStreamSynchronize(g.s) != cudaSuccess) return LES_ERR_CUDA;
+    for (auto &p : changed) {
+      les_batch::Group &g = b->groups[p.g];
+      if (les_sor_batch_upload(std::move(p.host), std::move(p.owner), g.sh, g.nmaxp, &g.buf) != 0) return LES_ERR_NOMEM;
+    }
+  }
   b->key = key;
   return LES_OK;
 }

@@ -21,6 +21,8 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cstring>
 #include <vector>
 
 #include "les_common.cuh"
@@ -140,14 +142,15 @@ bool les_sor_batch_ok(const LesDom &d, SorShape sh, const LesSorMaps *maps) {
          d.jm % 2 == 0 && d.km + 1 < LES_SOR_KMAX;
 }
 
-int les_sor_batch_prepare(const std::vector<const LesDom *> &doms, const std::vector<const LesSorMaps *> &maps,
-                          SorShape sh, int nmaxp, SorBatchBuffers *buf) {
+bool les_sor_batch_build(const std::vector<const LesDom *> &doms, const std::vector<const LesSorMaps *> &maps,
+                         SorShape sh, int nmaxp, const SorBatchBuffers &buf, std::vector<SorBatchDom> *host,
+                         std::vector<int> *owner) {
   const int n = (int)doms.size();
-  std::vector<SorBatchDom> host(n);
-  std::vector<int> owner;
+  host->assign(n, SorBatchDom{});  // value-initialised: padding zero, so tables compare bytewise
+  owner->clear();
   int first = 0;
   for (int m = 0; m < n; ++m) {
-    SorBatchDom &M = host[m];
+    SorBatchDom &M = (*host)[m];
     M.mA = maps[m]->m[0];
     M.mB = maps[m]->m[1];
     M.mR = maps[m]->m[2];
@@ -156,9 +159,17 @@ int les_sor_batch_prepare(const std::vector<const LesDom *> &doms, const std::ve
     M.tiles_x = (doms[m]->im + (4 * sh.nx - 8) - 1) / (4 * sh.nx - 8);
     M.ntiles = les_sor_fused_tiles(doms[m]->im, doms[m]->jm, one);
     M.first = first;
-    for (int t = 0; t < M.ntiles; ++t) owner.push_back(m);
+    for (int t = 0; t < M.ntiles; ++t) owner->push_back(m);
     first += M.ntiles;
   }
+  return !(buf.nmaxp == nmaxp && buf.shape.nx == sh.nx && buf.shape.ny == sh.ny && buf.owner_host == *owner &&
+           buf.host.size() == host->size() &&
+           (host->empty() || memcmp(buf.host.data(), host->data(), sizeof(SorBatchDom) * host->size()) == 0));
+}
+
+int les_sor_batch_upload(std::vector<SorBatchDom> host, std::vector<int> owner, SorShape sh, int nmaxp,
+                         SorBatchBuffers *buf) {
+  const int n = (int)host.size();
   // (re)allocate on growth
   if (buf->cap_dom < n || buf->cap_owner < (int)owner.size()) {
     cudaFree(buf->doms);
@@ -177,15 +188,18 @@ int les_sor_batch_prepare(const std::vector<const LesDom *> &doms, const std::ve
       return -1;
     }
   }
-  if (cudaMemcpy(buf->doms, host.data(), sizeof(SorBatchDom) * n, cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemcpy(buf->owner, owner.data(), sizeof(int) * owner.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+  if ((n && cudaMemcpy(buf->doms, host.data(), sizeof(SorBatchDom) * n, cudaMemcpyHostToDevice) != cudaSuccess) ||
+      (!owner.empty() &&
+       cudaMemcpy(buf->owner, owner.data(), sizeof(int) * owner.size(), cudaMemcpyHostToDevice) != cudaSuccess)) {
     (void)cudaGetLastError();
     return -2;
   }
   buf->ndom = n;
-  buf->per_level = first;
+  buf->per_level = (int)owner.size();
   buf->nmaxp = nmaxp;
   buf->shape = sh;
+  buf->host = std::move(host);
+  buf->owner_host = std::move(owner);
   return 0;
 }
 

@@ -29,7 +29,8 @@ struct SorBatchArgs {
   int hold_member;      // test hook: this member's first level waits on a count never reached (-1: none)
 };
 
-// Device buffers of one batched launch group (one tile shape).
+// Device buffers of one batched launch group (one tile shape), with the host copies of
+// what was uploaded last.
 struct SorBatchBuffers {
   SorBatchDom *doms = nullptr;
   int *owner = nullptr;
@@ -37,15 +38,24 @@ struct SorBatchBuffers {
   int cap_dom = 0, cap_owner = 0;
   int ndom = 0, per_level = 0, nmaxp = 0;
   SorShape shape;
+  std::vector<SorBatchDom> host;
+  std::vector<int> owner_host;
 };
 
 // A member can take part in a batched SOR launch of shape sh: the one-iteration TMA
 // sweep applies (uniform cn1, omega = 1, even jm) and its maps are for sh.
 bool les_sor_batch_ok(const LesDom &d, SorShape sh, const LesSorMaps *maps);
-// Build the work list and member table of a group (synchronous upload: call it with no
-// launch of this group in flight).  0 on success.
-int les_sor_batch_prepare(const std::vector<const LesDom *> &doms, const std::vector<const LesSorMaps *> &maps,
-                          SorShape sh, int nmaxp, SorBatchBuffers *buf);
+// The member table and work list of a group, built on the host.  Returns true if they
+// differ from what buf holds (members, their domains' device views or tensor maps, the
+// shape or the iteration count): a handle freed and another created at the same address
+// is a different member.
+bool les_sor_batch_build(const std::vector<const LesDom *> &doms, const std::vector<const LesSorMaps *> &maps,
+                         SorShape sh, int nmaxp, const SorBatchBuffers &buf, std::vector<SorBatchDom> *host,
+                         std::vector<int> *owner);
+// Upload a built table and work list (synchronous: call it with no launch of this group
+// in flight).  0 on success.
+int les_sor_batch_upload(std::vector<SorBatchDom> host, std::vector<int> owner, SorShape sh, int nmaxp,
+                         SorBatchBuffers *buf);
 // Queue iterations 2..nmaxp of every member on stream s (the members' rhs, iteration 1
 // and sor_begin must precede it on s).  spin_limit bounds each dependency wait.
 int les_sor_batch_launch(const SorBatchBuffers &buf, int sms, long long spin_limit, int hold_member, cudaStream_t s);
