@@ -285,10 +285,11 @@ def _seconds_synced(fn):
     return time.perf_counter() - t0
 
 
-def ensemble(specs, warmup, steps, params=None):
+def ensemble(specs, warmup, steps, params=None, persistent=False):
     """Step scenarios together in one batch; returns (cell-steps/s, seconds per step).
     Timed on the host between full device synchronisations (the members run on many
-    streams)."""
+    streams).  persistent: SOR iterations 2..nmaxp of all members in one persistent
+    launch over their tiles (les_batch_set_sor_launch)."""
     import lesgpu
     params = params or lesgpu.Params()
     doms = []
@@ -298,7 +299,7 @@ def ensemble(specs, warmup, steps, params=None):
         doms.append(d)
     # SOR tile shape per size class, measured with the GPU shared (before any timing)
     lesgpu.tune_classes(doms, shared=True)
-    b = lesgpu.Batch()
+    b = lesgpu.Batch(persistent_sor=persistent)
     for d in doms:
         b.add(d, 1, 10**6)
     for _ in range(warmup):
@@ -356,24 +357,29 @@ def batched_lines(warmup=3, steps=10):
     """The two ensemble measurements carried by the headline line."""
     uni = uniform_specs()
     v_batch, s_step, bad = ensemble(uni, warmup, steps)
+    v_pers, s_pers, bad_p = ensemble(uni, warmup, steps, persistent=True)
     v_alone = one_by_one(uni[:1], warmup, steps)
-    batched = {"value": v_batch, "unit": UNIT, "ms_per_step": 1e3 * s_step, "nonfinite": bad,
+    batched = {"value": v_batch, "unit": UNIT, "ms_per_step": 1e3 * s_step, "nonfinite": bad + bad_p,
                "workload": "64 domains of 150x150x90, own building seed, inflow direction U[0,360), speed U[2,10] m/s",
                "plain_small_value": v_alone, "vs_plain_small": v_batch / v_alone,
+               "persistent_sor": {"value": v_pers, "ms_per_step": 1e3 * s_pers, "vs_plain_small": v_pers / v_alone,
+                                  "launch": "SOR iterations 2..nmaxp of all members in one persistent launch over "
+                                            "their tile work-list"},
                "timing": "host clock between device synchronisations, after warm-up"}
     une = uneven_specs()
     v_ub, s_ub, bad_u = ensemble(une, warmup, steps)
+    v_up, s_up, bad_up = ensemble(une, warmup, steps, persistent=True)
     v_obo = one_by_one(une, warmup, 3)
-    uneven = {"value": v_ub, "unit": UNIT, "ms_per_step": 1e3 * s_ub, "nonfinite": bad_u,
+    uneven = {"value": v_ub, "unit": UNIT, "ms_per_step": 1e3 * s_ub, "nonfinite": bad_u + bad_up,
               "workload": "96 domains, ip, jp in {64,96,128,192,256}, kp in {48,64,90}, coverage U[15,45]%",
               "cells": sum(sc.im * sc.jm * sc.km for sc in une), "one_by_one_value": v_obo,
-              "vs_one_by_one": v_ub / v_obo}
+              "vs_one_by_one": v_ub / v_obo,
+              "persistent_sor": {"value": v_up, "ms_per_step": 1e3 * s_up, "vs_one_by_one": v_up / v_obo}}
     return batched, uneven
 
 
 def run_ours(args):
     world, rank, local, pg = dist_setup()
-    pool = oracle_pool() if (rank == 0 and not args.no_serve) else None  # FP64 checks of served requests
     import numpy as np
     import torch
     torch.cuda.set_device(local)
@@ -423,7 +429,8 @@ def run_ours(args):
     # The read-back is les_gpu_download_async into pinned buffers (two sets, alternating):
     # the step's fields are snapshotted in stream order and copied while the next step
     # runs; step n's copies are waited for after step n+1 is queued, the last ones before
-    # the clock stops.
+    # the clock stops.  Three windows of e2e_steps steps are timed; the line reports the
+    # median window (host-side effects make single short windows vary by 10%).
     e2e_steps = max(3, min(args.steps, 20))
     zbm, uin, vin, win = lesgpu.generate_scenario(scenario(seed=1 + rank, im=IM, jm=JM, km=KM))
     pin = [torch.from_numpy(np.asfortranarray(a).ravel(order="F").copy()).pin_memory() for a in (uin, vin, win)]
@@ -434,26 +441,29 @@ def run_ours(args):
     lib = dom.lib
     iarr = lambda t: (C.c_int * 3)(*t)
     fptr = lambda t: C.cast(t.data_ptr(), C.POINTER(C.c_float))
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    prev = []
-    for q in range(e2e_steps):
-        for fid, t in zip((lesgpu.UIN, lesgpu.VIN, lesgpu.WIN), pin):
-            dom._check(lib.les_gpu_upload(dom._h, fid, fptr(t), iarr(lbi), iarr(ubi)), "upload inflow")
-        dom.step(n, nmax)
-        n += 1
-        cur = []
-        for fid, t in zip((lesgpu.U, lesgpu.V, lesgpu.W, lesgpu.P), outs[q % 2]):
-            tk = C.c_longlong(-1)
-            dom._check(lib.les_gpu_download_async(dom._h, fid, fptr(t), iarr(lb), iarr(ub), C.byref(tk)), "download")
-            cur.append(tk.value)
-        for tk in prev:  # the previous step's fields are now in host memory
+    windows = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        prev = []
+        for q in range(e2e_steps):
+            for fid, t in zip((lesgpu.UIN, lesgpu.VIN, lesgpu.WIN), pin):
+                dom._check(lib.les_gpu_upload(dom._h, fid, fptr(t), iarr(lbi), iarr(ubi)), "upload inflow")
+            dom.step(n, nmax)
+            n += 1
+            cur = []
+            for fid, t in zip((lesgpu.U, lesgpu.V, lesgpu.W, lesgpu.P), outs[q % 2]):
+                tk = C.c_longlong(-1)
+                dom._check(lib.les_gpu_download_async(dom._h, fid, fptr(t), iarr(lb), iarr(ub), C.byref(tk)),
+                           "download")
+                cur.append(tk.value)
+            for tk in prev:  # the previous step's fields are now in host memory
+                dom._check(lib.les_gpu_download_wait(dom._h, tk), "download_wait")
+            prev = cur
+        for tk in prev:
             dom._check(lib.les_gpu_download_wait(dom._h, tk), "download_wait")
-        prev = cur
-    for tk in prev:
-        dom._check(lib.les_gpu_download_wait(dom._h, tk), "download_wait")
-    e2e_s = time.perf_counter() - t0
-    e2e_s = reduce_max(pg, e2e_s)
+        windows.append(reduce_max(pg, time.perf_counter() - t0))
+    e2e_s = sorted(windows)[1]
     e2e_val = world * cells * e2e_steps / e2e_s
     h2d = 3 * JM * KM * 4
     d2h = 4 * cells * 4
@@ -506,7 +516,8 @@ def run_ours(args):
                 "data": "synthetic: seeded urban heightmap and power-law inflow (no dataset in the reference)",
                 "config": workload_config(IM, JM, KM), "clocks": clk.summary(),
                 "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                        "steps": e2e_steps,
+                        "steps": e2e_steps, "windows_ms_per_step": [1e3 * w / e2e_steps for w in windows],
+                        "window": "median of three windows",
                         "read_back": "les_gpu_download_async of interior u, v, w, p every step (snapshot in "
                                      "stream order, copy overlapping the next step), all waited for"},
                 "gpu_launches": launches, "nonfinite": bad, "roofline": roofline, "cpu_baseline": cpu,
@@ -517,6 +528,7 @@ def run_ours(args):
             except Exception as e:  # the ensembles must not sink the headline line
                 line["batched"] = {"failed": str(e)}
         if not args.no_serve:
+            pool = oracle_pool()  # FP64 checks of served requests (spawned: safe with the GPU in use)
             try:
                 line["serve"] = serve_lines(pool)
             except Exception as e:  # the serving run must not sink the headline line
@@ -530,9 +542,12 @@ def run_ours(args):
 
 
 def _oracle_check(job):
-    """FP64 oracle run of one served scenario to its final step (runs in a spawned
-    worker process; the scenario comes from the oracle's own generator): the max
-    relative error of the GPU's final u, v, w, p."""
+    """Oracle runs of one served scenario to its final step (in a spawned worker process;
+    the scenario comes from the oracle's own generator): the max relative error of the
+    GPU's final u, v, w, p against the FP64 oracle and against the FP32 restatement with
+    the GPU's arithmetic (IEEE x**0.5, FP64-accurate sums), and the FP32 restatement's
+    own distance from FP64 -- the drift of the reference's precision over the run, which
+    on long chaotic runs alone exceeds 1e-4."""
     sc_kw, nsteps, gpu_fields = job
     import numpy as np
 
@@ -540,16 +555,29 @@ def _oracle_check(job):
     oref.set_threads(2)
     zbm, uin, vin, win = oref.scenario(fast=True, **sc_kw)
     im, jm, km = sc_kw["im"], sc_kw["jm"], sc_kw["km"]
-    r = oref.Ref(8, im, jm, km, zbm, uin, vin, win, dx=sc_kw["dx"], dy=sc_kw["dy"], dz_law=sc_kw["dz_law"],
-                 dz0=sc_kw["dz0"], dz_ratio=sc_kw["dz_ratio"], sqrt_half=0, red64=1, fast=True)
+    kw = dict(dx=sc_kw["dx"], dy=sc_kw["dy"], dz_law=sc_kw["dz_law"], dz0=sc_kw["dz0"], dz_ratio=sc_kw["dz_ratio"],
+              fast=True)
+    r64 = oref.Ref(8, im, jm, km, zbm, uin, vin, win, sqrt_half=0, red64=1, **kw)
+    r32 = oref.Ref(4, im, jm, km, zbm, uin, vin, win, sqrt_half=1, red64=1, **kw)
     for n in range(1, nsteps + 1):
-        r.step(n, nsteps)
-    err = 0.0
+        r64.step(n, nsteps)
+        r32.step(n, nsteps)
+
+    def rel(a, b):
+        return float(np.abs(a.astype(np.float64) - b).max() / max(np.abs(b).max(), 1e-30))
+
+    out = {"gpu_vs_fp64": 0.0, "gpu_vs_fp32": 0.0, "fp32_vs_fp64": 0.0}
     for fid, g in gpu_fields.items():
-        o = r.get(fid, (1, 1, 1), (im, jm, km))
-        err = max(err, float(np.abs(g.astype(np.float64) - o).max() / max(np.abs(o).max(), 1e-30)))
-    r.close()
-    return err
+        o64 = r64.get(fid, (1, 1, 1), (im, jm, km))
+        o32 = r32.get(fid, (1, 1, 1), (im, jm, km))
+        out["gpu_vs_fp64"] = max(out["gpu_vs_fp64"], rel(g, o64))
+        out["gpu_vs_fp32"] = max(out["gpu_vs_fp32"], rel(g, o32))
+        out["fp32_vs_fp64"] = max(out["fp32_vs_fp64"], rel(o32, o64))
+    r64.close()
+    r32.close()
+    out["steps"] = nsteps
+    out["cells"] = im * jm * km
+    return out
 
 
 def oracle_pool():
@@ -594,13 +622,20 @@ def serve_window(rate, seconds, seed, pool, sample_every=20, max_check=None):
 
 
 def serve_summary(st, checks):
-    errs = [c.get() for c in checks]
+    res = [c.get() for c in checks]
     keep = ("rate_hz", "window_s", "requests", "completed", "rejected", "wall_s", "drain_s", "cell_steps_per_s",
             "latency_s", "service_s", "queue_wait_s", "max_backlog", "mean_live_cells", "clocks")
     out = {k: st[k] for k in keep}
-    out["oracle_check"] = {"requests": len(errs), "max_rel_err": max(errs) if errs else None, "tolerance": 1e-4,
-                           "sample": "every 20th request (5 percent); u, v, w, p at the request's final step vs the "
-                                     "FP64 oracle"}
+    g64 = [x["gpu_vs_fp64"] for x in res]
+    out["oracle_check"] = {
+        "requests": len(res), "max_rel_err": max(g64) if g64 else None, "tolerance": 1e-4,
+        "within_tolerance": sum(1 for e in g64 if e <= 1e-4),
+        "max_vs_fp32_restatement": max((x["gpu_vs_fp32"] for x in res), default=None),
+        "reference_precision_drift": [{"steps": x["steps"], "cells": x["cells"], "gpu_vs_fp64": x["gpu_vs_fp64"],
+                                       "fp32_vs_fp64": x["fp32_vs_fp64"]} for x in res],
+        "sample": "every 20th request (5 percent); u, v, w, p at the request's final step vs the FP64 oracle and "
+                  "vs the FP32 restatement; fp32_vs_fp64 is the reference precision's own distance from FP64 "
+                  "over the same run"}
     return out
 
 

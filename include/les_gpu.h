@@ -257,12 +257,17 @@ int les_batch_admit(const les_dims *dims, size_t reserve_bytes, int *ok);
 int les_batch_add(les_batch *b, les_handle *h, int n0, int nmax, int *slot);
 int les_batch_remove(les_batch *b, int slot);  /* syncs the member first */
 /* One step of every unfinished member; *nlive = members with steps left after it.
- * Each member's step runs up to its first SOR iteration on its own stream; SOR
- * iterations 2..nmaxp of all members (of one tile shape) then run as one persistent
- * launch over a work-list of every member's tiles, whose CTAs wait (bounded) for a
- * member's previous iteration before its next; the rest of each step follows on the
- * member's stream.  Members without a fused SOR sweep step alone. */
+ * By default each member's whole-step graph runs on its own stream.  With
+ * les_batch_set_sor_launch(b, 1), each member's step runs up to its first SOR iteration
+ * on its own stream; SOR iterations 2..nmaxp of all members (of one tile shape) then
+ * run as one persistent launch over a work-list of every member's tiles, whose CTAs
+ * wait (bounded) for a member's previous iteration before its next; the rest of each
+ * step follows on the member's stream (members without a fused SOR sweep step alone).
+ * Either way a member's fields are bitwise those of the domain stepped alone. */
 int les_batch_step(les_batch *b, int *nlive);
+/* persistent = 1: the persistent SOR launch over all members' tiles; 0 (default): each
+ * member's whole-step graph on its own stream.  No counterpart in the reference. */
+int les_batch_set_sor_launch(les_batch *b, int persistent);
 /* Waits for every member; fails with LES_ERR_STATE if a dependency wait of a batched
  * SOR launch gave up since the last call (the members' SOR of that step is incomplete). */
 int les_batch_sync(les_batch *b);

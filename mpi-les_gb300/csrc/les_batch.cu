@@ -3,19 +3,23 @@
 //
 // A batch holds domain handles (each with its own device state, CUDA stream and
 // captured step graphs) and a per-slot step counter.  les_batch_step enqueues one time
-// step of every live member without host synchronisation:
-//   1. each member's step up to its first SOR iteration (a captured graph on the
-//      member's stream; the members' kernels overlap on the GPU);
-//   2. SOR iterations 2..nmaxp of all members at once: one persistent launch per tile
-//      shape over a work-list of every member's tiles (les_sor_batch.cu), on a stream of
-//      the batch that waits for step 1 of its members;
-//   3. each member's copy-out, pav and boundary conditions (a captured graph on the
-//      member's stream, after the batched launch).
-// A member whose SOR cannot take part (no fused sweep: odd jm, km too large; a state
-// just uploaded) steps through its own whole-step graph.  Members join and leave
-// between steps (continuous batching); nothing in a member's arithmetic depends on the
-// others, so a domain's result is the same alone and in any mix, bit for bit.  Calls on
-// one batch are serialised by its mutex.
+// step of every live member without host synchronisation, in one of two ways:
+//   - (default) each member's whole-step graph on its own stream: the members' kernels
+//     overlap on the GPU (a 150x150x90 domain fills a fraction of the 152 SMs per
+//     kernel, many of them fill it);
+//   - (les_batch_set_sor_launch(b, 1)) SOR iterations 2..nmaxp of all members as one
+//     persistent launch per tile shape over a work-list of every member's tiles
+//     (les_sor_batch.cu): each member's step runs up to its first SOR iteration on its
+//     own stream (a captured graph), the batched launch waits for them on the batch's
+//     stream, and each member's copy-out, pav and boundary conditions follow it.
+//     Members without a fused SOR sweep (odd jm, km too large, a state just uploaded)
+//     step through their whole-step graph.  Measured on a GB300 it is 7% (64 domains of
+//     150x150x90) and 9% (96 uneven domains) slower than the default: each member's
+//     first part must finish before the launch starts, and every item of the work-list
+//     pays its own pipeline start.
+// Members join and leave between steps (continuous batching); nothing in a member's
+// arithmetic depends on the others, so a domain's result is the same alone and in any
+// mix, bit for bit, either way.  Calls on one batch are serialised by its mutex.
 //
 // Concurrency across streams is limited by CUDA_DEVICE_MAX_CONNECTIONS (8 unless the
 // process sets it, before CUDA initialises, up to 32).  Members share the GPU, so
@@ -24,6 +28,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <map>
 #include <mutex>
 #include <string>
@@ -60,6 +65,12 @@ struct les_batch {
   std::vector<Group> groups;
   std::vector<std::tuple<int, les_handle *, int, int, int>> key;  // (slot, handle, nx, ny, nmaxp) of the groups
   long long spin_limit = 1LL << 23;  // polls (about 128 ns each) before a dependency wait gives up
+  cudaStream_t bs = nullptr;         // the stream of the batched SOR launches
+  int group_size = 1 << 30;          // members per batched SOR launch (LES_BATCH_GROUP overrides);
+                                     // concurrent persistent launches starve each other, so one
+                                     // launch per shape is the default
+  bool batched_sor = false;          // true: SOR iterations 2..nmaxp of all members in one
+                                     // persistent launch (les_batch_set_sor_launch; LES_BATCH_SOR)
   int hold_slot = -1;                // test hook: this member's wait can never end
   int sms = 0;
   std::mutex mu;
@@ -76,6 +87,11 @@ int bfail(les_batch *b, int code, const std::string &m) {
 extern "C" int les_batch_create(les_batch **out) {
   if (!out) return LES_ERR_ARG;
   *out = new les_batch();
+  if (const char *e = getenv("LES_BATCH_GROUP")) {  // A/B measurements
+    const int v = atoi(e);
+    if (v > 0) (*out)->group_size = v;
+  }
+  if (const char *e = getenv("LES_BATCH_SOR")) (*out)->batched_sor = atoi(e) != 0;
   return LES_OK;
 }
 
@@ -88,11 +104,11 @@ extern "C" int les_batch_destroy(les_batch *b) {
     for (auto &g : b->groups) {
       if (g.s) cudaStreamSynchronize(g.s);
       les_sor_batch_free(&g.buf);
-      if (g.s) cudaStreamDestroy(g.s);
       if (g.done) cudaEventDestroy(g.done);
     }
     for (auto &s : b->slots)
       if (s.ev) cudaEventDestroy(s.ev);
+    if (b->bs) cudaStreamDestroy(b->bs);
   }
   delete b;
   return LES_OK;
@@ -150,8 +166,19 @@ namespace {
 // the launches in flight finish before the new tables are uploaded.
 int regroup(les_batch *b, const std::vector<std::tuple<int, les_handle *, int, int, int>> &key,
             const std::vector<const LesDom *> &doms, const std::vector<const LesSorMaps *> &maps) {
-  std::map<std::tuple<int, int, int>, std::vector<int>> by;  // (nx, ny, nmaxp) -> indices into key
-  for (int q = 0; q < (int)key.size(); ++q) by[{std::get<2>(key[q]), std::get<3>(key[q]), std::get<4>(key[q])}].push_back(q);
+  // (nx, ny, nmaxp, chunk) -> indices into key.  Members of one shape are split into
+  // chunks of at most group_size: each chunk's launch waits only for its own members'
+  // first part, so one chunk's SOR overlaps the other chunks' remaining kernels.
+  std::map<std::tuple<int, int, int>, std::vector<int>> shape;
+  for (int q = 0; q < (int)key.size(); ++q)
+    shape[{std::get<2>(key[q]), std::get<3>(key[q]), std::get<4>(key[q])}].push_back(q);
+  std::map<std::tuple<int, int, int, int>, std::vector<int>> by;
+  for (auto &kv : shape) {
+    const int n = (int)kv.second.size();
+    const int nch = std::max(1, (n + b->group_size - 1) / b->group_size);
+    for (int q = 0; q < n; ++q)
+      by[{std::get<0>(kv.first), std::get<1>(kv.first), std::get<2>(kv.first), q * nch / n}].push_back(kv.second[q]);
+  }
   while (b->groups.size() < by.size()) b->groups.emplace_back();
   struct Pending {
     size_t g;
@@ -162,7 +189,8 @@ int regroup(les_batch *b, const std::vector<std::tuple<int, les_handle *, int, i
   size_t gi = 0;
   for (auto &kv : by) {
     les_batch::Group &g = b->groups[gi];
-    if (!g.s && cudaStreamCreateWithFlags(&g.s, cudaStreamNonBlocking) != cudaSuccess) return LES_ERR_CUDA;
+    if (!b->bs && cudaStreamCreateWithFlags(&b->bs, cudaStreamNonBlocking) != cudaSuccess) return LES_ERR_CUDA;
+    g.s = b->bs;  // one stream: the batched launches never run side by side (they would starve each other)
     if (!g.done && cudaEventCreateWithFlags(&g.done, cudaEventDisableTiming) != cudaSuccess) return LES_ERR_CUDA;
     const SorShape sh{std::get<0>(kv.first), std::get<1>(kv.first), 0, 1};
     const int nmaxp = std::get<2>(kv.first);
@@ -226,7 +254,7 @@ extern "C" int les_batch_step(les_batch *b, int *nlive) {
     const LesSorMaps *mp = nullptr;
     int nmaxp = 0, ok = 0;
     les_handle_batch_view(s.h, &d, &sh, &mp, &nmaxp, &streams[q], &ok);
-    if (!ok || nmaxp < 2) {
+    if (!ok || nmaxp < 2 || !b->batched_sor) {
       alone.push_back(q);
       continue;
     }
@@ -275,6 +303,13 @@ extern "C" int les_batch_step(les_batch *b, int *nlive) {
     if (s.n <= s.nmax) ++live;
   }
   if (nlive) *nlive = live;
+  return LES_OK;
+}
+
+extern "C" int les_batch_set_sor_launch(les_batch *b, int persistent) {
+  if (!b || persistent < 0 || persistent > 1) return LES_ERR_ARG;
+  std::lock_guard<std::mutex> lock(b->mu);
+  b->batched_sor = persistent != 0;
   return LES_OK;
 }
 

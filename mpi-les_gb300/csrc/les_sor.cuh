@@ -16,7 +16,8 @@ struct SorArgs {
   int ntiles;            // CTAs in the launch
   double *part;          // per-CTA residual partials (>= ntiles)
   unsigned int *counter; // CTA completion ticket, zero between launches
-  int ghost;             // 1: also write pdst's periodic ghost rows (internal buffers)
+  int ghost;             // also write pdst's periodic ghost rows (internal buffers): 1 two
+                         // rows per side, 2 four (read by two-iteration marches, jm >= 4)
   int kchunk;            // k planes per CTA (grid z = nchunk chunks); >= km: one chunk
   int nchunk;            // chunks (grid z)
   int depth = 1;         // iterations this launch performs (1, or 2: les_sor2.cu)

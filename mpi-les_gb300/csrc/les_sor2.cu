@@ -354,7 +354,7 @@ void launch2(const LesDom &d, const SorArgs &a, const CUtensorMap &tp, const CUt
 bool les_sor_two_ok(const LesDom &d, SorShape sh) {
   return sh.depth == 2 && sh.nx == 32 && (sh.ny == 24 || sh.ny == 28 || sh.ny == 32) &&
          (sh.kchunk <= 0 || sh.kchunk >= d.km) && d.gr.cn1k && !d.cn1 && d.omega == 1.f && d.sor_uni &&
-         d.km + 1 < LES_SOR_KMAX && d.jm % 2 == 0;
+         d.km + 1 < LES_SOR_KMAX && d.jm % 2 == 0 && d.jm >= 4;
 }
 
 void les_launch_sor_iter2(const LesDom &d, const SorArgs &a, int ny, const CUtensorMap &tp, const CUtensorMap &tr,

@@ -45,17 +45,24 @@ template <int NX, int NY, int D>
 __global__ void __launch_bounds__(NX *NY, min_ctas(NX)) k_sor_batch(SorBatchArgs B) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   TmaSmem<NX, NY, D> &S = *reinterpret_cast<TmaSmem<NX, NY, D> *>(smem_raw);
+  // the item: its index, whether to compute it, its member's domain view and the
+  // iteration's arguments, all in shared memory at fixed addresses, so the march holds
+  // no extra live registers for them
   __shared__ unsigned s_item;
-  __shared__ int s_work;  // 1: compute the item; 0: count it only (member converged)
+  __shared__ int s_work, s_m;
+  __shared__ LesDom s_d;
+  __shared__ __align__(16) unsigned char s_a_raw[sizeof(SorArgs)];  // SorArgs has member initialisers
+  SorArgs &s_a = *reinterpret_cast<SorArgs *>(s_a_raw);
   const int tid = threadIdx.y * NX + threadIdx.x;
   const unsigned total = (unsigned)B.per_level * (unsigned)B.levels;
   for (;;) {
     if (tid == 0) {
       unsigned t = atomicAdd(B.queue, 1u);
       if (t < total && *(volatile int *)B.status) t = total;  // a wait gave up: stop
-      int work = 0;
+      int work = 0, m = 0;
       if (t < total) {
-        const int lvl = (int)(t / (unsigned)B.per_level), m = B.owner[t % (unsigned)B.per_level];
+        const int lvl = (int)(t / (unsigned)B.per_level);
+        m = B.owner[t % (unsigned)B.per_level];
         const SorBatchDom &M = B.doms[m];
         // level lvl needs every tile of level lvl-1; the test hook holds one member's
         // level 1 on a count that is never reached
@@ -80,43 +87,58 @@ __global__ void __launch_bounds__(NX *NY, min_ctas(NX)) k_sor_batch(SorBatchArgs
           const CUtensorMap *mp = (l & 1) ? &M.mA : &M.mB;
           asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(mp) : "memory");
           asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(&M.mR) : "memory");
+          if (work) {
+            const LesDom &d = M.d;
+            const bool last = (l == B.nmaxp);
+            SorArgs a;
+            a.psrc = (l & 1) ? d.sorA : d.sorB;  // iteration l-1 wrote sorB if l-1 is odd
+            a.pdst = last ? d.p : ((l & 1) ? d.sorB : d.sorA);
+            a.dstcode = last ? 2 : ((l & 1) ? 1 : 0);
+            a.ghost = last ? 0 : 1;
+            a.rhs = d.sorR;
+            a.tj = NY - 4;
+            a.kchunk = d.km;
+            a.nchunk = 1;
+            a.ntiles = M.ntiles;
+            a.part = d.part;
+            a.counter = d.cnt;
+            s_a = a;
+          }
         }
       }
       s_item = t;
       s_work = work;
+      s_m = m;
     }
     __syncthreads();
     const unsigned t = s_item;
     if (t >= total) break;
-    const int lvl = (int)(t / (unsigned)B.per_level), r = (int)(t % (unsigned)B.per_level);
-    const int m = B.owner[r];
-    const SorBatchDom &M = B.doms[m];
     if (s_work) {
-      const LesDom &d = M.d;
-      const int l = lvl + 2;  // the SOR iteration (iteration 1 read p, in the member's own stream)
-      const bool last = (l == B.nmaxp);
-      SorArgs a;
-      a.psrc = (l & 1) ? d.sorA : d.sorB;  // iteration l-1 wrote sorB if l-1 is odd
-      a.pdst = last ? d.p : ((l & 1) ? d.sorB : d.sorA);
-      a.dstcode = last ? 2 : ((l & 1) ? 1 : 0);
-      a.ghost = last ? 0 : 1;
-      a.rhs = d.sorR;
-      a.tj = NY - 4;
-      a.kchunk = d.km;
-      a.nchunk = 1;
-      a.ntiles = M.ntiles;
-      a.part = d.part;
-      a.counter = d.cnt;
-      const int tile = r - M.first;
-      sor_tma_tile<NX, NY, D, false>(d, a, (l & 1) ? &M.mA : &M.mB, &M.mR, tile % M.tiles_x, tile / M.tiles_x, 0,
-                                     tile, S);
+      {  // the member's domain view into shared memory, word by word
+        const unsigned *src = reinterpret_cast<const unsigned *>(&B.doms[s_m].d);
+        unsigned *dst = reinterpret_cast<unsigned *>(&s_d);
+        for (int w = tid; w < (int)(sizeof(LesDom) / 4); w += NX * NY) dst[w] = src[w];
+      }
+      __syncthreads();
+      auto item_tile = [&]() {
+        const int r = (int)(s_item % (unsigned)B.per_level);
+        return r - B.doms[s_m].first;
+      };
+      auto maps = [&](int which) -> const CUtensorMap * {
+        const SorBatchDom &M = B.doms[s_m];
+        if (which) return &M.mR;
+        const int l = (int)(s_item / (unsigned)B.per_level) + 2;
+        return (l & 1) ? &M.mA : &M.mB;
+      };
+      const int tile = item_tile(), tx = B.doms[s_m].tiles_x;
+      sor_tma_tile<NX, NY, D, false>(s_d, s_a, maps, tile % tx, tile / tx, 0, item_tile, S);
     }
     __syncthreads();
     if (tid == 0) {
       if (s_work)
         for (int q = 0; q < D; ++q) mbar_inval(&S.bar[q]);  // quiescent: re-initialised by the next item
       __threadfence();
-      atomicAdd(B.done + m, 1u);
+      atomicAdd(B.done + s_m, 1u);
     }
   }
 }

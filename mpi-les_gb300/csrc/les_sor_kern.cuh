@@ -107,12 +107,17 @@ struct Lane {
   bool row_owned, row_red, col_owned, owned, west0;
   int east_e;
   bool ival[4];
-  unsigned gmask;  // ghost rows that copy row jr (ghost_mask)
+  // periodic ghost rows that copy row jr (NO_GHOST: none): rows jm+1.., -1.. for the
+  // two-row ghost band (SorArgs.ghost 1), jm+1..jm+4, -3..0 for the four-row band
+  // (ghost 2, jm >= 4: at most two per row).  Held as two precomputed rows: a general
+  // loop over the candidates costs the sweep 3% (97.5 against 100.6 us per iteration).
+  int ghost1, ghost2;
 };
 
-// bx, by: the tile's column and row in the domain's tile grid
+// bx, by: the tile's column and row in the domain's tile grid; ghost: SorArgs.ghost
+constexpr int NO_GHOST = -1000;
 template <int NX>
-__device__ __forceinline__ Lane make_lane(const LesDom &d, int tj, int ny, int bx, int by) {
+__device__ __forceinline__ Lane make_lane(const LesDom &d, int tj, int ny, int bx, int by, int ghost) {
   Lane L;
   L.c4 = threadIdx.x;
   // 16-column tiles: a warp holds two rows two apart (rows 0,2 | 1,3 | 4,6 | 5,7 ...), so
@@ -134,7 +139,9 @@ __device__ __forceinline__ Lane make_lane(const LesDom &d, int tj, int ny, int b
   L.east_e = d.im - L.ib;
 #pragma unroll
   for (int e = 0; e < 4; ++e) L.ival[e] = (L.ib + e >= 1) && (L.ib + e <= d.im);
-  L.gmask = ghost_mask(L.jr, d.jm);
+  const int band = (ghost == 2) ? 4 : 2;
+  L.ghost1 = (L.jr <= band && L.jr >= 1) ? L.jr + d.jm : NO_GHOST;
+  L.ghost2 = (L.jr > d.jm - band && L.jr <= d.jm) ? L.jr - d.jm : NO_GHOST;
   return L;
 }
 
@@ -153,7 +160,10 @@ __device__ __forceinline__ void store_final(const LesDom &d, const SorArgs &a, c
     }
   };
   put(L.jr);
-  if (a.ghost) for_ghost_rows(d.jm, L.gmask, [&](int off) { put(L.jr + off); });
+  if (a.ghost) {
+    if (L.ghost1 != NO_GHOST) put(L.ghost1);
+    if (L.ghost2 != NO_GHOST) put(L.ghost2);
+  }
 }
 
 // FP32 (Kahan) per thread -> FP64 per CTA -> last CTA sums the CTA partials in order.
@@ -227,7 +237,7 @@ __global__ void __launch_bounds__(NX *NY, min_ctas(NX)) k_sor_reg(LesDom d, SorA
   // must be cut back to its first iteration
   if (a.redo ? d.ctl[CT_REDO] == 0 : d.ctl[CT_CONVERGED] != 0) return;
 
-  const Lane L = make_lane<NX>(d, a.tj, NY, blockIdx.x, blockIdx.y);
+  const Lane L = make_lane<NX>(d, a.tj, NY, blockIdx.x, blockIdx.y, a.ghost);
   const int c4 = L.c4, r = L.r, ib = L.ib, jw = L.jw;
   const int im = d.im, jm = d.jm, km = d.km;
   const bool col_load = (ib <= im + 1);
@@ -449,15 +459,17 @@ struct TmaSmem {
   int last, abort_;
 };
 
-// One tile of one iteration: tile (bx, by) of the domain's tile grid, k chunk bz, partial
-// slot cta; tmP / tmR: tensor maps of the source p buffer and of rhs (kernel parameters
-// or global memory).  Every thread of the CTA calls it; it leaves the mbarriers
-// quiescent (every copy it issued has been waited for).
-template <int NX, int NY, int D, bool KC>
-__device__ __forceinline__ void sor_tma_tile(const LesDom &d, const SorArgs &a, const CUtensorMap *tmP,
-                                             const CUtensorMap *tmR, int bx, int by, int bz, int cta,
-                                             TmaSmem<NX, NY, D> &S) {
-  const Lane L = make_lane<NX>(d, a.tj, NY, bx, by);
+// One tile of one iteration, for the batched launch (les_sor_batch.cu): tile (bx, by) of
+// the domain's tile grid, k chunk bz.  maps(0) / maps(1) give the tensor maps of the
+// source p buffer and of rhs, and cta() the tile's partial slot; both are evaluated
+// where they are used rather than held across the march (a value held live across the
+// march measurably slows it: 6% for the partial slot alone).  Every thread of the CTA
+// calls it; it leaves the mbarriers quiescent (every copy it issued has been waited
+// for).  k_sor_tma below is the same sweep written out for one domain per launch.
+template <int NX, int NY, int D, bool KC, class MapFn, class CtaFn>
+__device__ __forceinline__ void sor_tma_tile(const LesDom &d, const SorArgs &a, MapFn maps, int bx, int by, int bz,
+                                             CtaFn cta, TmaSmem<NX, NY, D> &S) {
+  const Lane L = make_lane<NX>(d, a.tj, NY, bx, by, a.ghost);
   const int c4 = L.c4, r = L.r, ib = L.ib, jw = L.jw;
   const int km = d.km;
   float c2l[4], c2s[4];
@@ -485,8 +497,8 @@ __device__ __forceinline__ void sor_tma_tile(const LesDom &d, const SorArgs &a, 
   auto issue = [&](int m) {  // plane m (mfirst..mlast) into stage (m - mfirst) % D
     const int q = (m - mfirst) % D;
     mbar_expect_tx(&S.bar[q], stage_bytes);
-    tma_load_3d(&S.p[q][0][0], tmP, tx, ty, m + LES_KOFF, &S.bar[q]);
-    tma_load_3d(&S.rhs[q][0][0], tmR, tx, ty, m + LES_KOFF, &S.bar[q]);
+    tma_load_3d(&S.p[q][0][0], maps(0), tx, ty, m + LES_KOFF, &S.bar[q]);
+    tma_load_3d(&S.rhs[q][0][0], maps(1), tx, ty, m + LES_KOFF, &S.bar[q]);
   };
 
   if (producer) {
@@ -632,7 +644,7 @@ __device__ __forceinline__ void sor_tma_tile(const LesDom &d, const SorArgs &a, 
     for (int m = failed_at; m <= mlast && m < failed_at + D; ++m)
       (void)mbar_wait(&S.bar[(m - mfirst) % D], (uint32_t)(((m - mfirst) / D) & 1));
   }
-  finish_residual<NX, NY>(d, a, acc, S.warp, &S.last, cta);
+  finish_residual<NX, NY>(d, a, acc, S.warp, &S.last, cta());
 }
 
 template <int NX, int NY, int D, bool KC>
@@ -643,8 +655,183 @@ __global__ void __launch_bounds__(NX *NY, min_ctas(NX))
   // early exit of press.f95:119-121; in redo mode: run only when a two-iteration launch
   // must be cut back to its first iteration
   if (a.redo ? d.ctl[CT_REDO] == 0 : d.ctl[CT_CONVERGED] != 0) return;
-  sor_tma_tile<NX, NY, D, KC>(d, a, &tmP, &tmR, blockIdx.x, blockIdx.y, blockIdx.z,
-                              (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x, S);
+
+  const Lane L = make_lane<NX>(d, a.tj, NY, blockIdx.x, blockIdx.y, a.ghost);
+  const int c4 = L.c4, r = L.r, ib = L.ib, jw = L.jw;
+  const int km = d.km;
+  float c2l[4], c2s[4];
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    c2l[e] = L.ival[e] ? d.gr.cn2l[ib + e] : 0.f;
+    c2s[e] = L.ival[e] ? d.gr.cn2s[ib + e] : 0.f;
+  }
+  const float c3l = d.gr.cn3l[jw], c3s = d.gr.cn3s[jw];
+  const float rhsav = d.fscal[SC_RHSAV];
+  // omega = 1 (press.f95:45, the only value this kernel is launched for): omega * x is x
+  constexpr float omega = 1.f;
+  const bool producer = (r == 0) && (c4 == 0);
+  const int tx = blockIdx.x * tile_i(NX);  // padded column of i0 - 4
+  const int ty = blockIdx.y * a.tj + (LES_JOFF - 1);  // padded row of j0 - 2
+  const uint32_t stage_bytes = 2u * NY * NX * 16u;
+  // this CTA's k chunk [ka, kb], marched from ka-1 (a red ring plane) to kb+1; it
+  // loads planes mfirst .. mlast, plane m into stage (m - mfirst) % D
+  const int ka = KC ? 1 + (int)blockIdx.z * a.kchunk : 1;
+  const int kb = KC ? min(km, ka + a.kchunk - 1) : km;
+  const int s_begin = KC ? max(1, ka - 1) : 1;
+  const int s_end = KC ? min(km + 1, kb + 1) : km + 1;
+  const int mfirst = KC ? max(1, s_begin - 1) : 1;
+  const int mlast = KC ? min(km, kb + 2) : km;
+  auto issue = [&](int m) {  // plane m (mfirst..mlast) into stage (m - mfirst) % D
+    const int q = (m - mfirst) % D;
+    mbar_expect_tx(&S.bar[q], stage_bytes);
+    tma_load_3d(&S.p[q][0][0], &tmP, tx, ty, m + LES_KOFF, &S.bar[q]);
+    tma_load_3d(&S.rhs[q][0][0], &tmR, tx, ty, m + LES_KOFF, &S.bar[q]);
+  };
+
+  if (producer) {
+    for (int q = 0; q < D; ++q) mbar_init(&S.bar[q], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    S.abort_ = 0;
+  }
+  for (int q = r * NX + c4; q <= km; q += NX * NY) {
+    if (q >= 1) {
+      S.c4l[q] = d.gr.cn4l[q];
+      S.c4s[q] = d.gr.cn4s[q];
+      S.ck[q] = d.gr.cn1k[q];
+    }
+  }
+  __syncthreads();
+  if (producer)
+    for (int m = mfirst; m < mfirst + D && m <= mlast; ++m) issue(m);
+
+  int failed_at = 0;
+  // plane m sits in stage (m - mfirst) % D with mbarrier phase parity ((m - mfirst) / D) & 1
+  auto wait_stage = [&](int m, int st, uint32_t ph) {
+    if (!mbar_wait(&S.bar[st], ph)) {
+      S.abort_ = 1;
+      d.ctl[CT_ERROR] = 1;
+      if (!failed_at) failed_at = m;
+    }
+  };
+  auto wait_plane = [&](int m) { wait_stage(m, (m - mfirst) % D, (uint32_t)(((m - mfirst) / D) & 1)); };
+
+  // Plane m of p lives in register slot P[m % 4] and its rhs and coefficients in slot
+  // m % 2; the march is unrolled 4 times so every slot is a compile-time register and
+  // the planes never move between registers.  Plane 0 reads as plane 1 (boundp2's
+  // Neumann copy): with slot s_begin-1 a copy of plane 1 taken before its red update,
+  // every k-halo read below finds the cell's own current value (red at s = 1 reads that
+  // copy, black at k = 1 reads it one step later, and at the top the slot of plane
+  // km+1 is a copy of plane km), so the march needs no halo selects.
+  const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  float4 P[4], R[2];
+  float CK[2] = {0.f, 0.f}, C4L[2] = {0.f, 0.f}, C4S[2] = {0.f, 0.f};
+#pragma unroll
+  for (int t = 0; t < 4; ++t) P[t] = zero4;
+  R[0] = R[1] = zero4;
+  {
+    wait_plane(s_begin);
+    const float4 p0 = S.p[(s_begin - mfirst) % D][r][c4];
+    float4 pm1 = p0;
+    if (KC && s_begin > 1) {
+      wait_plane(s_begin - 1);
+      pm1 = S.p[(s_begin - 1 - mfirst) % D][r][c4];
+    }
+    const int t0 = s_begin % 4, t1 = (s_begin + 3) % 4;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      if (t == t0) P[t] = p0;
+      if (t == t1) P[t] = pm1;
+    }
+  }
+  // residual: plain FP32 sums over a group of four steps, Kahan-compensated across groups
+  float acc = 0.f, comp = 0.f, grp = 0.f;
+  auto fold_group = [&]() {
+    const float y = grp - comp;
+    const float t = acc + y;
+    comp = (t - acc) - y;
+    acc = t;
+    grp = 0.f;
+  };
+  // stage and phase of plane s (st0) and of plane s+1 (st1, ph1), advanced per step
+  int st0 = (s_begin - mfirst) % D, st1 = (s_begin + 1 - mfirst) % D;
+  uint32_t ph1 = (uint32_t)(((s_begin + 1 - mfirst) / D) & 1);
+
+  // residual weights: red counts the owned cells of the tile, black runs on owned
+  // threads only
+  float mred[4], mblack[4];
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    mblack[e] = L.ival[e] ? 1.f : 0.f;
+    mred[e] = (L.owned && L.ival[e]) ? 1.f : 0.f;
+  }
+
+  auto step = [&](auto UC, int s) {
+    constexpr int U = decltype(UC)::value;  // s = U modulo 4
+    constexpr int S0 = U, SP1 = (U + 1) % 4, SM1 = (U + 3) % 4, SM2 = (U + 2) % 4;
+    constexpr int C0 = U % 2, CM = (U + 1) % 2;
+    if (s < s_begin) return;  // before this chunk's start (the unrolled march is aligned to 4)
+    __syncthreads();
+    if (S.abort_) return;
+    // the stage of plane s-1 is free: every thread has left step s-1 (or the prologue)
+    if (producer && s - 1 >= mfirst && s - 1 + D <= mlast) issue(s - 1 + D);
+    P[SP1] = P[S0];  // plane km+1 reads as plane km, before its red update
+    R[C0] = zero4;
+    if (s + 1 <= mlast) {
+      wait_stage(s + 1, st1, ph1);
+      P[SP1] = S.p[st1][r][c4];
+    }
+    float part = 0.f;
+    const int q = (jw + s) & 1;
+    const float rpl = __shfl_up_sync(0xffffffffu, P[S0].w, 1, NX);
+    const float rpr = __shfl_down_sync(0xffffffffu, P[S0].x, 1, NX);
+    const float bpl = __shfl_up_sync(0xffffffffu, P[SM1].w, 1, NX);
+    const float bpr = __shfl_down_sync(0xffffffffu, P[SM1].x, 1, NX);
+    // ---- red cells of plane s on the tile + 1-cell ring
+    if (s <= km) {
+      CK[C0] = S.ck[s];
+      C4L[C0] = S.c4l[s];
+      C4S[C0] = S.c4s[s];
+      if (L.row_red) {
+        R[C0] = S.rhs[st0][r][c4];
+        const float4 pn = S.p[st0][r + 1][c4], pso = S.p[st0][r - 1][c4];
+        const float pr_ = relax_pair_m(q, P[S0], rpl, rpr, pn, pso, P[SP1], P[SM1], R[C0], rhsav, omega, CK[C0], c2l,
+                                       c2s, c3l, c3s, C4L[C0], C4S[C0], L.west0, L.east_e, mred);
+        if (!KC || (s >= ka && s <= kb)) part += pr_;
+      }
+    }
+    S.red[U & 1][r][c4] = P[S0];
+    // ---- black cells of plane s-1 on the tile
+    if ((KC ? (s - 1 >= ka && s - 1 <= kb) : (s >= 2)) && L.owned) {
+      const int k = s - 1;
+      const float4 pn = S.red[(U + 1) & 1][r + 1][c4], pso = S.red[(U + 1) & 1][r - 1][c4];
+      part += relax_pair_m(q, P[SM1], bpl, bpr, pn, pso, P[S0], P[SM2], R[CM], rhsav, omega, CK[CM], c2l, c2s, c3l,
+                           c3s, C4L[CM], C4S[CM], L.west0, L.east_e, mblack);
+      store_final(d, a, L, k, P[SM1]);
+    }
+    grp += part;
+    st0 = st1;
+    if (++st1 == D) {
+      st1 = 0;
+      ph1 ^= 1u;
+    }
+  };
+  for (int s0 = s_begin - s_begin % 4; s0 <= s_end; s0 += 4) {
+    step(IC<0>{}, s0);
+    if (s0 + 1 > s_end) break;
+    step(IC<1>{}, s0 + 1);
+    if (s0 + 2 > s_end) break;
+    step(IC<2>{}, s0 + 2);
+    if (s0 + 3 > s_end) break;
+    step(IC<3>{}, s0 + 3);
+    fold_group();
+  }
+  fold_group();  // the last, partial group
+  // after a failed wait, wait (bounded) for the copies already issued before leaving
+  if (failed_at) {
+    for (int m = failed_at; m <= mlast && m < failed_at + D; ++m)
+      (void)mbar_wait(&S.bar[(m - mfirst) % D], (uint32_t)(((m - mfirst) / D) & 1));
+  }
+  finish_residual<NX, NY>(d, a, acc, S.warp, &S.last, (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x);
 }
 
 template <int NX, int NY, bool KC>

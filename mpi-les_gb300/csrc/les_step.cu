@@ -140,7 +140,7 @@ static void enqueue_sor_fused(const LesDom &d, const les_params &prm, SorShape s
     const bool last = (lend == nit) && (nit > 1);
     a.pdst = last ? d.p : ((cur == d.sorB) ? d.sorA : d.sorB);
     a.dstcode = last ? 2 : (a.pdst == d.sorA ? 0 : 1);
-    a.ghost = last ? 0 : 1;
+    a.ghost = last ? 0 : (two_ok ? 2 : 1);  // a two-iteration plan reads four ghost rows
     a.rhs = d.sorR;
     a.depth = two ? 2 : 1;
     a.tj = use.ny - 4 * a.depth;

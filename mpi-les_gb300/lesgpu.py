@@ -220,6 +220,7 @@ def load_library(path: str | None = None) -> C.CDLL:
         "les_batch_sync": (C.c_int, [vp]),
         "les_batch_slot": (C.c_int, [vp, C.c_int, ip_, ip_]),
         "les_batch_set_wait_limit": (C.c_int, [vp, C.c_longlong, C.c_int]),
+        "les_batch_set_sor_launch": (C.c_int, [vp, C.c_int]),
         "les_batch_last_error": (C.c_int, [vp, C.c_char_p, C.c_size_t]),
     }
     for name, (res, args) in sig.items():
@@ -552,17 +553,19 @@ class Domain:
 
 
 class Batch:
-    """Many resident domains stepped together (les_batch_*): each member's step on its own
-    stream around one persistent SOR launch over all members' tiles, members joining and
-    leaving between steps."""
+    """Many resident domains stepped together (les_batch_*), members joining and leaving
+    between steps: each member's whole-step graph on its own stream, or (persistent_sor)
+    each member's step around one persistent SOR launch over all members' tiles."""
 
-    def __init__(self):
+    def __init__(self, persistent_sor: bool = False):
         self.lib = load_library()
         self._b = C.c_void_p()
         rc = self.lib.les_batch_create(C.byref(self._b))
         if rc:
             raise RuntimeError(f"les_batch_create failed ({rc})")
         self.members: dict[int, Domain] = {}
+        if persistent_sor:
+            self.set_sor_launch(True)
 
     def _check(self, rc: int, what: str):
         if rc:
@@ -598,6 +601,11 @@ class Batch:
 
     def sync(self):
         self._check(self.lib.les_batch_sync(self._b), "sync")
+
+    def set_sor_launch(self, persistent: bool) -> None:
+        """True: SOR iterations 2..nmaxp of all members in one persistent launch over their
+        tiles; False (default): each member's whole-step graph on its own stream."""
+        self._check(self.lib.les_batch_set_sor_launch(self._b, 1 if persistent else 0), "set_sor_launch")
 
     def set_wait_limit(self, polls: int, hold_slot: int = -1) -> None:
         """Bound the batched SOR launch's dependency waits (polls of about 128 ns); a

@@ -27,14 +27,15 @@ def _same(a, b, what):
         assert np.array_equal(x.view(np.uint32), y.view(np.uint32)), (what, lesgpu.FIELD_NAMES[fid])
 
 
-def test_batch_member_same_alone_and_in_mix(built_lib):
+@pytest.mark.parametrize("persistent", [False, True])
+def test_batch_member_same_alone_and_in_mix(built_lib, persistent):
     params = lesgpu.Params(nmaxp=8)
     sa = scenario(48, 30, 14, seed=81, direction_deg=30.0, u_ref=4.0)
     sb = scenario(64, 40, 12, seed=82, direction_deg=200.0, u_ref=8.0)
     sc_ = scenario(37, 18, 11, seed=83, direction_deg=95.0)  # odd jm: the per-subroutine SOR path
     ref_a = _alone(sa, params, 6)
     ref_c = _alone(sc_, params, 4)
-    b = lesgpu.Batch()
+    b = lesgpu.Batch(persistent_sor=persistent)
     a, bb, c = make_gpu(sa, params), make_gpu(sb, params), make_gpu(sc_, params)
     sa_slot = b.add(a, 1, 6)
     b.add(bb, 1, 9)
@@ -134,7 +135,7 @@ def test_batched_sor_groups_and_fallbacks_match_alone(built_lib):
             d.step(n, 5)
         d.sync()
         alone.append(d)
-    b = lesgpu.Batch()
+    b = lesgpu.Batch(persistent_sor=True)
     doms = []
     for sc, shape in specs:
         d = make_gpu(sc, params)
@@ -163,7 +164,7 @@ def test_batched_sor_wait_gives_up_and_reports(built_lib):
     on a count nothing reaches) gives up after its bound, the launch stops, and
     les_batch_sync reports it; the GPU stays usable and the next batch steps normally."""
     params = lesgpu.Params(nmaxp=6)
-    b = lesgpu.Batch()
+    b = lesgpu.Batch(persistent_sor=True)
     doms = [make_gpu(scenario(64, 40, 12, seed=311 + q), params) for q in range(2)]
     slots = [b.add(d, 1, 3) for d in doms]
     b.set_wait_limit(1 << 14, hold_slot=slots[0])  # about 2 ms of polling
@@ -175,7 +176,7 @@ def test_batched_sor_wait_gives_up_and_reports(built_lib):
     # a fresh batch on the same GPU: steps and matches the domain alone
     sc = scenario(64, 40, 12, seed=321)
     ref = _alone(sc, params, 3)
-    b2 = lesgpu.Batch()
+    b2 = lesgpu.Batch(persistent_sor=True)
     d = make_gpu(sc, params)
     b2.add(d, 1, 3)
     while b2.step() > 0:

@@ -51,13 +51,14 @@ def test_bench_domain_600x600x90_vs_fp64(built_lib):
     assert max(errs.values()) <= 1e-4, errs
 
 
-def test_uniform_batch_members_150x150x90_vs_fp64(built_lib):
+@pytest.mark.parametrize("persistent", [False, True])
+def test_uniform_batch_members_150x150x90_vs_fp64(built_lib, persistent):
     import random
     rng = random.Random(2024)
     scs = [scenario(150, 150, 90, seed=rng.getrandbits(48), direction_deg=rng.uniform(0.0, 360.0),
                     u_ref=rng.uniform(2.0, 10.0)) for _ in range(3)]
     params = lesgpu.Params()
-    b = lesgpu.Batch()
+    b = lesgpu.Batch(persistent_sor=persistent)
     doms = [make_gpu(sc, params) for sc in scs]
     for d in doms:
         b.add(d, 1, 20)

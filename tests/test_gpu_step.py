@@ -141,12 +141,13 @@ def test_sor_shape_rejects_unbuilt_shapes(built_lib):
 
 
 @pytest.mark.parametrize("nmaxp", [2, 3, 8, 9, 50])
-@pytest.mark.parametrize("shape", [(150, 60, 20), (64, 2, 12), (40, 4, 7)])
+@pytest.mark.parametrize("shape", [(150, 60, 20), (64, 6, 12), (40, 4, 7), (64, 2, 12)])
 def test_two_iteration_sor_matches_one_iteration(built_lib, nmaxp, shape):
     """Two SOR iterations per k-march give the fields of one iteration per launch bit
     for bit, for even and odd iteration counts (a one-iteration launch before or after
-    the pairs), partial tiles, jm = 2 and 4 (every ghost row a copy of a copy), and the
-    residual of the last iteration within summation-order rounding."""
+    the pairs), partial tiles, jm = 4 and 6 (ghost rows that are copies of copies), and
+    the residual of the last iteration within summation-order rounding.  jm = 2 (too
+    narrow for the four-row ghost band) runs one iteration per launch."""
     sc = scenario(*shape, seed=75)
     params = lesgpu.Params(nmaxp=nmaxp)
 
@@ -159,7 +160,7 @@ def test_two_iteration_sor_matches_one_iteration(built_lib, nmaxp, shape):
         return d
 
     a, b = run(1), run(2)
-    assert b.sor_shape()[3] == 2
+    assert b.sor_shape()[3] == (2 if sc.jm >= 4 else 1)
     for fid in lesgpu.STATE_FIELDS:
         x, y = a.download(fid), b.download(fid)
         assert np.array_equal(x.view(np.uint32), y.view(np.uint32)), (nmaxp, lesgpu.FIELD_NAMES[fid])
