@@ -184,3 +184,33 @@ def test_batched_sor_wait_gives_up_and_reports(built_lib):
     b2.sync()
     _same(d, ref, "after a failed wait")
     b2.close()
+
+
+def test_batched_sor_member_replaced_matches_alone(built_lib):
+    """A finished member removed and destroyed, then a new domain of the same shape
+    created (its handle and device buffers may take the freed addresses) and added to
+    the same persistent-SOR batch: the batch rebuilds its member table for the new
+    domain, which ends bitwise equal to the same scenario stepped alone."""
+    params = lesgpu.Params(nmaxp=8)
+    sa = scenario(64, 40, 12, seed=331, direction_deg=20.0)
+    sb = scenario(64, 40, 12, seed=332, direction_deg=160.0, u_ref=7.0)
+    keep = scenario(48, 32, 12, seed=333)
+    ref_b = _alone(sb, params, 4)
+    ref_k = _alone(keep, params, 7)
+    b = lesgpu.Batch(persistent_sor=True)
+    a = make_gpu(sa, params)
+    k = make_gpu(keep, params)
+    sa_slot = b.add(a, 1, 3)
+    b.add(k, 1, 7)
+    for _ in range(3):
+        b.step()
+    b.sync()
+    b.remove(sa_slot).close()
+    d = make_gpu(sb, params)
+    b.add(d, 1, 4)
+    while b.step() > 0:
+        pass
+    b.sync()
+    _same(d, ref_b, "replacement")
+    _same(k, ref_k, "kept member")
+    b.close()
