@@ -213,6 +213,9 @@ int les_gpu_boundp2(les_handle *h);                  /* boundp.f95:7  */
 int les_gpu_step(les_handle *h, int n, int nmax);
 /* Steps n0 .. n0+nsteps-1 back to back (the main.f95:247 loop body). */
 int les_gpu_run(les_handle *h, int n0, int nsteps, int nmax);
+/* Waits for the handle's stream.  LES_ERR_STATE if a kernel since the last sync gave
+ * up a bounded wait for its own copies (never expected; the results of that work are
+ * void, and the flag is cleared). */
 int les_gpu_sync(les_handle *h);
 /* Diagnostics of the last press call: out[0] SOR iterations, out[1] last residual
  * sum (FP64), out[2] uout, out[3] rhsav, out[4] pav.  Synchronises. */
@@ -269,7 +272,8 @@ int les_batch_step(les_batch *b, int *nlive);
  * member's whole-step graph on its own stream.  No counterpart in the reference. */
 int les_batch_set_sor_launch(les_batch *b, int persistent);
 /* Waits for every member; fails with LES_ERR_STATE if a dependency wait of a batched
- * SOR launch gave up since the last call (the members' SOR of that step is incomplete). */
+ * SOR launch gave up since the last call (the members' SOR of that step is incomplete),
+ * or if a member's own kernel gave up a bounded wait (as les_gpu_sync reports it). */
 int les_batch_sync(les_batch *b);
 /* Bound of the batched SOR launch's dependency waits, in polls of about 128 ns (default
  * 2^23, about a second).  hold_slot >= 0 makes that member's wait impossible, so that a

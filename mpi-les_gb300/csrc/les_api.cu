@@ -925,9 +925,31 @@ extern "C" int les_gpu_run(les_handle *h, int n0, int nsteps, int nmax) {
   return LES_OK;
 }
 
+// For les_batch.cu: the member's stream alone, and clearing its give-up word after the
+// batch has reported the failure itself.
+int les_handle_sync_stream(les_handle *h) {
+  CK(h, cudaStreamSynchronize(h->s));
+  return LES_OK;
+}
+void les_handle_clear_wait_error(les_handle *h) {
+  if (h->ctl_d) {
+    cudaMemsetAsync(h->ctl_d + CT_ERROR, 0, sizeof(int), h->s);
+    cudaStreamSynchronize(h->s);
+  }
+}
+
 extern "C" int les_gpu_sync(les_handle *h) {
   if (!h) return LES_ERR_ARG;
   CK(h, cudaStreamSynchronize(h->s));
+  if (h->ctl_d) {  // a kernel whose bounded wait gave up: the work since the last sync is void
+    int err = 0;
+    CK(h, cudaMemcpyAsync(&err, h->ctl_d + CT_ERROR, sizeof err, cudaMemcpyDeviceToHost, h->s));
+    CK(h, cudaStreamSynchronize(h->s));
+    if (err) {
+      les_handle_clear_wait_error(h);
+      return fail(h, LES_ERR_STATE, "a kernel's bounded wait for its copies gave up; the steps since the last sync are void");
+    }
+  }
   return LES_OK;
 }
 

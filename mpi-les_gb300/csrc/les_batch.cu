@@ -44,6 +44,8 @@ void les_handle_share_gpu(les_handle *h);
 int les_handle_batch_view(les_handle *h, const LesDom **d, SorShape *sh, const LesSorMaps **maps, int *nmaxp,
                           cudaStream_t *s, int *ok);
 int les_handle_step_part(les_handle *h, int n, int part);
+int les_handle_sync_stream(les_handle *h);
+void les_handle_clear_wait_error(les_handle *h);
 
 struct les_batch {
   struct Slot {
@@ -327,7 +329,7 @@ extern "C" int les_batch_sync(les_batch *b) {
   for (int q = 0; q < (int)b->slots.size(); ++q) {
     auto &s = b->slots[q];
     if (!s.used) continue;
-    const int rc = les_gpu_sync(s.h);
+    const int rc = les_handle_sync_stream(s.h);
     if (rc) return bfail(b, rc, "batch_sync: slot " + std::to_string(q));
   }
   for (auto &g : b->groups) {
@@ -338,9 +340,21 @@ extern "C" int les_batch_sync(les_batch *b) {
       // clear the record, so that later steps report only their own failures
       if (g.buf.counters) cudaMemsetAsync(g.buf.counters + 1, 0, sizeof(unsigned), g.s);
       cudaStreamSynchronize(g.s);
+      for (auto &s : b->slots)
+        if (s.used) les_handle_clear_wait_error(s.h);
       return bfail(b, LES_ERR_STATE,
                    "batch_sync: a dependency wait of the batched SOR launch gave up; the members' SOR of that step "
-                   "did not finish (their CT_ERROR word is set)");
+                   "did not finish");
+    }
+  }
+  for (int q = 0; q < (int)b->slots.size(); ++q) {  // a member kernel's own give-up
+    auto &s = b->slots[q];
+    if (!s.used) continue;
+    const int rc = les_gpu_sync(s.h);
+    if (rc) {
+      char msg[256] = {0};
+      les_gpu_last_error(s.h, msg, sizeof msg);
+      return bfail(b, rc, "batch_sync: slot " + std::to_string(q) + ": " + msg);
     }
   }
   return LES_OK;

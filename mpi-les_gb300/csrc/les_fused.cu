@@ -21,10 +21,16 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdint>
 #include <cstdlib>
+#include <map>
+#include <mutex>
+#include <vector>
 
 #include "les_common.cuh"
 #include "les_kernels.cuh"
+#include "les_sor.cuh"
+#include "les_tma.cuh"
 
 namespace {
 
@@ -948,6 +954,200 @@ __global__ void __launch_bounds__(VTX *VTY) k_les_visc_fix(LesDom d, uint3 g) {
 }
 
 
+// ---- the halo entries of diu that les reads through index remaps ----------------------
+// The copies vel2.f95:202-318 makes, written into the stored arrays after velfg (and its
+// fixup) so that the TMA-fed march reads plain boxes: diu1, diu4, diu7 at i = im+1 (the
+// values at i = im), diu2, diu5, diu8 at j = jm+1 (at j = 1), diu4 at j = 0 (at j = jm)
+// for k = 1..km, diu6 at j = 0 for k = 2..km+1, and diu4 at (im+1, 0) (at (im, jm)).  The
+// other remapped entries read as zero (diu2, diu3 at i = 0; diu7, diu8 at k = 0; diu9 at
+// k = km+1): nothing writes them, and the arrays start zeroed.  One thread per face
+// point (jm of the i face, im of the j faces, the corner), one block row per plane.
+__global__ void k_diu_halo(LesDom d) {
+  const int k = blockIdx.y + 1;  // 1 .. km+1
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int jmp = d.jm * d.pi;
+  if (t < d.jm) {
+    if (k > d.km) return;
+    const int c = lix(d, d.im, t + 1, k);
+    d.diu[1][c + 1] = d.diu[1][c];
+    d.diu[4][c + 1] = d.diu[4][c];
+    d.diu[7][c + 1] = d.diu[7][c];
+  } else if (t < d.jm + d.im) {
+    const int i = t - d.jm + 1;
+    if (k <= d.km) {
+      const int c1 = lix(d, i, 1, k);
+      d.diu[2][c1 + jmp] = d.diu[2][c1];
+      d.diu[5][c1 + jmp] = d.diu[5][c1];
+      d.diu[8][c1 + jmp] = d.diu[8][c1];
+      const int cm = lix(d, i, d.jm, k);
+      d.diu[4][cm - jmp] = d.diu[4][cm];
+    }
+    if (k >= 2) {
+      const int cm = lix(d, i, d.jm, k);
+      d.diu[6][cm - jmp] = d.diu[6][cm];
+    }
+  } else if (t == d.jm + d.im && k <= d.km) {
+    const int c = lix(d, d.im, d.jm, k);
+    d.diu[4][c + 1 - jmp] = d.diu[4][c];
+  }
+}
+
+// ---- the TMA-fed viscous march -------------------------------------------------------
+// k_les_visc_march with its planes brought into shared memory by tensor copies instead
+// of loads staged through registers.  k_diu_halo has stored the halo entries of the diu
+// arrays that les reads through index remaps, so every plane the march reads is a plain
+// box of a padded array: sm and diu1..9 as 40 x 10 boxes (i0-3 .. i0+36, the
+// tile's columns with their one-cell ring widened to 16-byte boundaries; rows j0 ..
+// j0+9), f, g, h (and fold, gold, hold with adam) as 32 x 8 boxes of the tile's cells.
+// Stage kk of the ring holds sm(kk+1), diu1,2,4,5,7,8(kk), diu3,6,9(kk+1) and the
+// cells' arrays at kk; step k reads stages k, k-1 and k-2, and once every thread has
+// finished step k the freed slot takes stage k+1+VLA, so the copies of VLA steps are
+// in flight while a step computes.  Warp 0 issues a stage (one copy per lane) after
+// lane 0 has armed the stage's mbarrier with the bytes to expect; every thread waits
+// (bounded) for the stages it reads.  The arithmetic is visc_compute's, so the fields
+// are bitwise those of k_les_visc_march.
+constexpr int VBW = 40, VHB = VBW * VTH, VHS = 416, VCB = VTX * VTY;  // VHS: slot stride (128-byte multiple)
+struct ViscStage {
+  float h[10][VHS];  // [0] sm(kk+1); [n] diu_n at kk (n = 1, 2, 4, 5, 7, 8) or kk+1 (n = 3, 6, 9)
+  float c[6][VCB];   // f, g, h, fold, gold, hold at kk
+};
+struct LesViscMaps {
+  CUtensorMap m[16];  // sm, diu1..9, f, g, h, fold, gold, hold
+};
+template <int VLA>
+struct ViscSmem {
+  ViscStage st[3 + VLA];
+  uint64_t bar[3 + VLA];
+};
+
+template <bool P2, bool ZF, bool AD, int VLA>
+__global__ void __launch_bounds__(VTX *VTY, 2) k_les_visc_tma(LesDom d, const __grid_constant__ LesViscMaps M) {
+  extern __shared__ __align__(1024) unsigned char vsm_raw[];
+  constexpr int NS = 3 + VLA;
+  constexpr int NMAP = AD ? 16 : 13;
+  ViscSmem<VLA> &S = *reinterpret_cast<ViscSmem<VLA> *>(vsm_raw);
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * VTX + tx;
+  const int i0 = blockIdx.x * VTX, j0 = blockIdx.y * VTY;  // tile origin (halo) at (i0, j0)
+  const int k0 = blockIdx.z * VKC + 1, k1 = min(k0 + VKC - 1, d.km);
+  const int i = i0 + tx + 1, j = j0 + ty + 1;
+  const bool in = (i <= d.im && j <= d.jm);
+  const int ic = min(i, d.im), jc = min(j, d.jm);
+  const int last_t = k1 - k0 + 2;  // stage t holds plane kk = k0 - 2 + t
+
+  // stage t into its slot: t = 0 needs only sm(k0-1), t = 1 sm(k0), diu3,6,9(k0), diu7,8(k0-1)
+  auto issue = [&](int t) {  // by the 32 lanes of warp 0
+    const int q = t % NS, kk = k0 - 2 + t;
+    const uint32_t mask = (t == 0) ? 0x1u : (t == 1) ? 0x3c9u : 0xffffu;  // maps issued
+    const uint32_t bytes = (t == 0) ? VHB * 4u : (t == 1) ? 6u * VHB * 4u : (10u * VHB + (NMAP - 10u) * VCB) * 4u;
+    if (tx == 0) mbar_expect_tx(&S.bar[q], bytes);
+    __syncwarp();
+    if (tx < NMAP && ((mask >> tx) & 1u)) {
+      if (tx < 10) {
+        const int z = (tx == 0 || tx == 3 || tx == 6 || tx == 9) ? kk + 1 : kk;
+        tma_load_3d(S.st[q].h[tx], &M.m[tx], i0, j0 + LES_JOFF, z + LES_KOFF, &S.bar[q]);
+      } else {
+        tma_load_3d(S.st[q].c[tx - 10], &M.m[tx], i0 + 1 + LES_IOFF, j0 + 1 + LES_JOFF, kk + LES_KOFF, &S.bar[q]);
+      }
+    }
+  };
+  if (tid == 0) {
+    for (int q = 0; q < NS; ++q) mbar_init(&S.bar[q], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  int issued = -1;
+  if (ty == 0)
+    for (int t = 0; t < NS && t <= last_t; ++t) {
+      issue(t);
+      issued = t;
+    }
+  // a wait that gives up sets CT_ERROR; this thread then skips its later waits (the
+  // step's results are void and reported) so the march still ends in bounded time
+  bool bad = false;
+  int waited = -1;
+  auto wait_stage = [&](int t) {
+    if (bad) return;
+    if (mbar_wait(&S.bar[t % NS], (uint32_t)((t / NS) & 1))) {
+      waited = t;
+    } else {
+      bad = true;
+      d.ctl[CT_ERROR] = 1;
+    }
+  };
+  const ViscCol cc = visc_col<P2>(d, ic, jc);
+  float ru = 0.f, rv = 0.f;
+  if (k0 == 1) {
+    ru = __ldg(&d.ruspd[(jc + LES_JOFF) * d.pi + ic + LES_IOFF]);
+    rv = __ldg(&d.rvspd[(jc + LES_JOFF) * d.pi + ic + LES_IOFF]);
+  }
+  int c = lix(d, ic, jc, k0);
+  wait_stage(0);
+  wait_stage(1);
+  const int o = (ty + 1) * VBW + tx + 4;  // this cell in a halo box
+  const int oc = ty * VTX + tx;           // and in a cell box
+  for (int k = k0; k <= k1; ++k) {
+    const int t = k - k0 + 2;
+    wait_stage(t);
+    const ViscStage &A = S.st[t % NS], &B = S.st[(t - 1) % NS], &C = S.st[(t - 2) % NS];
+#define HA(q, da, db) A.h[q][o + (db) * VBW + (da)]
+#define HB(q, da, db) B.h[q][o + (db) * VBW + (da)]
+#define HC(q, da, db) C.h[q][o + (db) * VBW + (da)]
+    ViscIn v;
+    v.s_c = HB(0, 0, 0); v.s_e = HB(0, 1, 0); v.s_w = HB(0, -1, 0);
+    v.s_n = HB(0, 0, 1); v.s_s = HB(0, 0, -1);
+    v.s_ne = HB(0, 1, 1); v.s_se = HB(0, 1, -1); v.s_nw = HB(0, -1, 1);
+    v.s_u = HA(0, 0, 0); v.s_eu = HA(0, 1, 0); v.s_wu = HA(0, -1, 0);
+    v.s_nu = HA(0, 0, 1); v.s_su = HA(0, 0, -1);
+    v.s_d = HC(0, 0, 0); v.s_ed = HC(0, 1, 0);
+    v.g1c = HA(1, 0, 0); v.g1e = HA(1, 1, 0);
+    v.g2c = HA(2, 0, 0); v.g2n = HA(2, 0, 1); v.g2wn = HA(2, -1, 1);
+    v.g3c = HB(3, 0, 0); v.g3u = HA(3, 0, 0); v.g3wu = HA(3, -1, 0);
+    v.g4c = HA(4, 0, 0); v.g4e = HA(4, 1, 0); v.g4es = HA(4, 1, -1);
+    v.g5c = HA(5, 0, 0); v.g5n = HA(5, 0, 1);
+    v.g6c = HB(6, 0, 0); v.g6u = HA(6, 0, 0); v.g6su = HA(6, 0, -1);
+    v.g7c = HA(7, 0, 0); v.g7e = HA(7, 1, 0); v.g7ed = HB(7, 1, 0);
+    v.g8c = HA(8, 0, 0); v.g8n = HA(8, 0, 1); v.g8nd = HB(8, 0, 1);
+    v.g9c = HB(9, 0, 0); v.g9u = HA(9, 0, 0);
+#undef HA
+#undef HB
+#undef HC
+    v.f0 = A.c[0][oc]; v.g0 = A.c[1][oc]; v.h0 = A.c[2][oc];
+    float fo = 0.f, go = 0.f, ho = 0.f;
+    if (AD) { fo = A.c[3][oc]; go = A.c[4][oc]; ho = A.c[5][oc]; }
+    v.ru = ru; v.rv = rv;
+    float fv, gv, hv;
+    unsigned bd = 0;
+    visc_compute<P2, ZF>(d, v, cc, visc_z(d, k), k, fv, gv, hv, bd);
+    // every thread is done with stage t-2: its slot takes stage t+1+VLA; a plane with a
+    // deferred cell is stored by the fixup
+    const bool defer = ZF && __syncthreads_or(in ? bd : 0u);
+    if (!ZF) __syncthreads();
+    if (ty == 0) {  // warp 0 (uniform: issue holds a __syncwarp); none of it issues after a failed wait
+      const bool wbad = __any_sync(0xffffffffu, bad);
+      if (!wbad && t + 1 + VLA <= last_t) {
+        issue(t + 1 + VLA);
+        issued = t + 1 + VLA;
+      }
+    }
+    if (defer) {
+      if (tid == 0) {
+        int *list = d.fix[FIX_VISC];
+        const int s = atomicAdd(list, 1);
+        list[2 + s] = (int)(((k - 1) * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x);
+      }
+    } else if (in) {
+      visc_store<AD>(d, c, fv, gv, hv, fo, go, ho);
+    }
+    c += d.np;
+    ru = 0.f;
+    rv = 0.f;
+  }
+  // after a wait gave up, wait (bounded) for the copies this warp issued before leaving
+  if (ty == 0 && bad)
+    for (int t = waited + 1; t <= issued; ++t) (void)mbar_wait(&S.bar[t % NS], (uint32_t)((t / NS) & 1));
+}
+
+
 }  // namespace
 
 #define LAUNCH(ctx, ...)                \
@@ -979,6 +1179,26 @@ void launch_variant(const LesDom &d, bool x, LesCtx ctx, dim3 g, dim3 b, Args...
              LAUNCH(ctx, (F<true, true>::fn<<<nfix, b, 0, ctx.s>>>(d, gu))); break;
   }
 }
+template <template <bool, bool, bool> class K, template <bool, bool> class F, typename... Args>
+void launch_variant_smem(const LesDom &d, bool x, LesCtx ctx, dim3 g, dim3 b, size_t smem, Args... args) {
+  const uint3 gu = make_uint3(g.x, g.y, g.z);
+  const unsigned nfix = std::min<unsigned>(g.x * g.y * g.z, (unsigned)std::max(1, 2 * d.sms));
+  const int v = (d.xy_pow2 ? 4 : 0) | (d.zfast ? 2 : 0) | (x ? 1 : 0);
+  switch (v) {
+    case 0: LAUNCH(ctx, (K<false, false, false>::fn<<<g, b, smem, ctx.s>>>(d, args...))); break;
+    case 1: LAUNCH(ctx, (K<false, false, true>::fn<<<g, b, smem, ctx.s>>>(d, args...))); break;
+    case 2: LAUNCH(ctx, (K<false, true, false>::fn<<<g, b, smem, ctx.s>>>(d, args...)));
+            LAUNCH(ctx, (F<false, false>::fn<<<nfix, b, 0, ctx.s>>>(d, gu))); break;
+    case 3: LAUNCH(ctx, (K<false, true, true>::fn<<<g, b, smem, ctx.s>>>(d, args...)));
+            LAUNCH(ctx, (F<false, true>::fn<<<nfix, b, 0, ctx.s>>>(d, gu))); break;
+    case 4: LAUNCH(ctx, (K<true, false, false>::fn<<<g, b, smem, ctx.s>>>(d, args...))); break;
+    case 5: LAUNCH(ctx, (K<true, false, true>::fn<<<g, b, smem, ctx.s>>>(d, args...))); break;
+    case 6: LAUNCH(ctx, (K<true, true, false>::fn<<<g, b, smem, ctx.s>>>(d, args...)));
+            LAUNCH(ctx, (F<true, false>::fn<<<nfix, b, 0, ctx.s>>>(d, gu))); break;
+    default: LAUNCH(ctx, (K<true, true, true>::fn<<<g, b, smem, ctx.s>>>(d, args...)));
+             LAUNCH(ctx, (F<true, true>::fn<<<nfix, b, 0, ctx.s>>>(d, gu))); break;
+  }
+}
 template <bool A, bool B, bool C>
 struct VelfgK {
   static constexpr auto fn = k_velfg_march<A, B, C>;
@@ -995,6 +1215,37 @@ template <bool A, bool C>
 struct ViscF {
   static constexpr auto fn = k_les_visc_fix<A, C>;
 };
+constexpr int kViscLookahead = 1;  // stages in flight beyond the three a step reads
+template <bool A, bool B, bool C>
+struct ViscTmaK {
+  static constexpr auto fn = k_les_visc_tma<A, B, C, kViscLookahead>;
+};
+
+// Tensor maps of the arrays the viscous march reads, cached per domain layout (the
+// maps hold only base addresses, extents and strides).
+bool visc_maps(const LesDom &d, LesViscMaps *out) {
+  static std::mutex mu;
+  static std::map<std::vector<uintptr_t>, LesViscMaps> cache;
+  const float *bases[16] = {d.sm, d.diu[1], d.diu[2], d.diu[3], d.diu[4], d.diu[5], d.diu[6], d.diu[7],
+                            d.diu[8], d.diu[9], d.f, d.g, d.h, d.fold, d.gold, d.hold};
+  std::vector<uintptr_t> key = {(uintptr_t)d.pi, (uintptr_t)d.nj, (uintptr_t)d.km};
+  for (const float *b : bases) key.push_back((uintptr_t)b);
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = cache.find(key);
+  if (it != cache.end()) {
+    *out = it->second;
+    return true;
+  }
+  LesViscMaps m;
+  for (int q = 0; q < 16; ++q) {
+    if (!bases[q] || ((uintptr_t)bases[q] & 15u)) return false;
+    if (les_tensor_map_3d(&m.m[q], d, bases[q], q < 10 ? VBW : VTX, q < 10 ? VTH : VTY) != 0) return false;
+  }
+  if (cache.size() >= 4096) cache.clear();
+  cache.emplace(key, m);
+  *out = m;
+  return true;
+}
 }  // namespace
 
 // Planes per block of the velfg march: chunks enough for about twelve blocks per SM,
@@ -1028,7 +1279,33 @@ void les_launch_les_fused(const LesDom &d, bool with_adam, LesCtx ctx) {
     LAUNCH(ctx, k_les_sm3<<<g, dim3(STX, STY), 0, ctx.s>>>(d, kc));
   }
   les_launch_boundsm(d, ctx);
-  // the k-march: 32 x 8 column tiles, chunks of VKC planes
+  // the k-march: 32 x 8 column tiles, chunks of VKC planes; TMA-fed when the arrays'
+  // tensor maps could be made (row pitch a multiple of 16 bytes), else register-staged
   const dim3 gv((d.im + VTX - 1) / VTX, (d.jm + VTY - 1) / VTY, (d.km + VKC - 1) / VKC);
+  static const int kind = [] {  // LES_VISC_KIND=0: the register-staged march (A/B measurements)
+    const char *e = getenv("LES_VISC_KIND");
+    return e ? atoi(e) : 1;
+  }();
+  LesViscMaps maps;
+  if (kind != 0 && (d.pi * 4) % 16 == 0 && visc_maps(d, &maps)) {
+    const size_t bytes = sizeof(ViscSmem<kViscLookahead>);
+    const int v = (d.xy_pow2 ? 4 : 0) | (d.zfast ? 2 : 0) | (with_adam ? 1 : 0);
+    auto set_attr = [&](const void *fn) {
+      cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    };
+    switch (v) {
+      case 0: set_attr((const void *)ViscTmaK<false, false, false>::fn); break;
+      case 1: set_attr((const void *)ViscTmaK<false, false, true>::fn); break;
+      case 2: set_attr((const void *)ViscTmaK<false, true, false>::fn); break;
+      case 3: set_attr((const void *)ViscTmaK<false, true, true>::fn); break;
+      case 4: set_attr((const void *)ViscTmaK<true, false, false>::fn); break;
+      case 5: set_attr((const void *)ViscTmaK<true, false, true>::fn); break;
+      case 6: set_attr((const void *)ViscTmaK<true, true, false>::fn); break;
+      default: set_attr((const void *)ViscTmaK<true, true, true>::fn); break;
+    }
+    LAUNCH(ctx, (k_diu_halo<<<dim3((d.im + d.jm + 1 + 255) / 256, d.km + 1), 256, 0, ctx.s>>>(d)));
+    launch_variant_smem<ViscTmaK, ViscF>(d, with_adam, ctx, gv, dim3(VTX, VTY), bytes, maps);
+    return;
+  }
   launch_variant<ViscK, ViscF>(d, with_adam, ctx, gv, dim3(VTX, VTY));
 }

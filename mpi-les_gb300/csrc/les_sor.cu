@@ -124,7 +124,7 @@ int les_sor_pick_kchunk(int tiles, int km, int sms) {
   return (km + nch - 1) / nch;
 }
 
-int les_sor_make_maps(const LesDom &d, SorShape sh, LesSorMaps *maps) {
+int les_tensor_map_3d(CUtensorMap *m, const LesDom &d, const float *base, int boxx, int boxy) {
   using EncodeFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
                                 const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -139,14 +139,19 @@ int les_sor_make_maps(const LesDom &d, SorShape sh, LesSorMaps *maps) {
   }
   const cuuint64_t dims[3] = {(cuuint64_t)d.pi, (cuuint64_t)d.nj, (cuuint64_t)(d.km + 4)};
   const cuuint64_t strides[2] = {(cuuint64_t)d.pi * 4u, (cuuint64_t)d.np * 4u};
-  const cuuint32_t box[3] = {(cuuint32_t)(sh.nx * 4), (cuuint32_t)sh.ny, 1u};
+  const cuuint32_t box[3] = {(cuuint32_t)boxx, (cuuint32_t)boxy, 1u};
   const cuuint32_t estr[3] = {1u, 1u, 1u};
-  float *bases[3] = {d.sorA, d.sorB, d.sorR};
+  const CUresult rc = encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(base), dims, strides, box,
+                             estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return rc == CUDA_SUCCESS ? 0 : -2;
+}
+
+int les_sor_make_maps(const LesDom &d, SorShape sh, LesSorMaps *maps) {
+  const float *bases[3] = {d.sorA, d.sorB, d.sorR};
   for (int q = 0; q < 3; ++q) {
-    CUresult rc = encode(&maps->m[q], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, bases[q], dims, strides, box, estr,
-                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (rc != CUDA_SUCCESS) return -2;
+    const int rc = les_tensor_map_3d(&maps->m[q], d, bases[q], sh.nx * 4, sh.ny);
+    if (rc != 0) return rc;
   }
   maps->shape = sh;
   maps->valid = 1;

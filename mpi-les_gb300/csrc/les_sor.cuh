@@ -50,6 +50,10 @@ SorShape les_sor_pick_shape(int im, int jm, int sms, bool shared_gpu);
 // fill them (each at least 8 planes: a chunk recomputes one red plane below it).
 int les_sor_pick_kchunk(int tiles, int km, int sms);
 int les_sor_make_maps(const LesDom &d, SorShape sh, LesSorMaps *maps);
+// A tiled tensor map of one padded 3-D field of the domain (float32; dims pi x nj x
+// km+4, its rows and planes as strides) with boxes of boxx x boxy x 1 (boxx * 4 bytes a
+// multiple of 16).  0 on success.
+int les_tensor_map_3d(CUtensorMap *m, const LesDom &d, const float *base, int boxx, int boxy);
 // One SOR iteration: the TMA kernel when the source is an internal buffer with valid
 // maps and cn1 is uniform, the register kernel otherwise.  With a.depth == 2 (only when
 // les_sor_two_ok holds): two iterations in one launch (les_sor2.cu).
