@@ -999,31 +999,32 @@ __global__ void k_diu_halo(LesDom d) {
 // box of a padded array: sm and diu1..9 as 40 x 10 boxes (i0-3 .. i0+36, the
 // tile's columns with their one-cell ring widened to 16-byte boundaries; rows j0 ..
 // j0+9), f, g, h (and fold, gold, hold with adam) as 32 x 8 boxes of the tile's cells.
-// Stage kk of the ring holds sm(kk+1), diu1,2,4,5,7,8(kk), diu3,6,9(kk+1) and the
-// cells' arrays at kk; step k reads stages k, k-1 and k-2, and once every thread has
-// finished step k the freed slot takes stage k+1+VLA, so the copies of VLA steps are
-// in flight while a step computes.  Warp 0 issues a stage (one copy per lane) after
-// lane 0 has armed the stage's mbarrier with the bytes to expect; every thread waits
-// (bounded) for the stages it reads.  The arithmetic is visc_compute's, so the fields
-// are bitwise those of k_les_visc_march.
+// Copy group kk brings sm(kk+1), diu1,2,4,5,7,8(kk), diu3,6,9(kk+1) and the cells'
+// arrays at kk; step k reads the groups of planes k, k-1 and k-2, and once every thread
+// has finished step k the group of plane k+1+VLA is issued, so the copies of VLA steps
+// are in flight while a step computes.  Each array has a ring of its own, as deep as its
+// reach: sm 3+VLA planes (read at k-1, k, k+1), diu3,6,9,7,8 2+VLA (two planes each),
+// diu1,2,4,5 and the cell arrays 1+VLA, so that three CTAs fit an SM's shared memory.  Warp 0 issues a group (one copy
+// per lane) after lane 0 has armed the group's mbarrier with the bytes to expect; every
+// thread waits (bounded) for the groups it reads.  The arithmetic is visc_compute's,
+// so the fields are bitwise those of k_les_visc_march.
 constexpr int VBW = 40, VHB = VBW * VTH, VHS = 416, VCB = VTX * VTY;  // VHS: slot stride (128-byte multiple)
-struct ViscStage {
-  float h[10][VHS];  // [0] sm(kk+1); [n] diu_n at kk (n = 1, 2, 4, 5, 7, 8) or kk+1 (n = 3, 6, 9)
-  float c[6][VCB];   // f, g, h, fold, gold, hold at kk
-};
 struct LesViscMaps {
   CUtensorMap m[16];  // sm, diu1..9, f, g, h, fold, gold, hold
 };
 template <int VLA>
 struct ViscSmem {
-  ViscStage st[3 + VLA];
-  uint64_t bar[3 + VLA];
+  float sm[3 + VLA][VHS];    // sm(kk+1) of group kk in slot kk % (3+VLA)
+  float z[5][2 + VLA][VHS];  // diu3, diu6, diu9 (at kk+1), diu7, diu8 (at kk)
+  float x[4][1 + VLA][VHS];  // diu1, diu2, diu4, diu5 (at kk)
+  float c[6][1 + VLA][VCB];  // f, g, h, fold, gold, hold (at kk)
+  uint64_t bar[3 + VLA];     // one per group in flight
 };
 
 template <bool P2, bool ZF, bool AD, int VLA>
-__global__ void __launch_bounds__(VTX *VTY, 2) k_les_visc_tma(LesDom d, const __grid_constant__ LesViscMaps M) {
+__global__ void __launch_bounds__(VTX *VTY, P2 ? 3 : 2) k_les_visc_tma(LesDom d, const __grid_constant__ LesViscMaps M) {
   extern __shared__ __align__(1024) unsigned char vsm_raw[];
-  constexpr int NS = 3 + VLA;
+  constexpr int NS = 3 + VLA, NZ = 2 + VLA, NX1 = 1 + VLA;
   constexpr int NMAP = AD ? 16 : 13;
   ViscSmem<VLA> &S = *reinterpret_cast<ViscSmem<VLA> *>(vsm_raw);
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * VTX + tx;
@@ -1032,9 +1033,9 @@ __global__ void __launch_bounds__(VTX *VTY, 2) k_les_visc_tma(LesDom d, const __
   const int i = i0 + tx + 1, j = j0 + ty + 1;
   const bool in = (i <= d.im && j <= d.jm);
   const int ic = min(i, d.im), jc = min(j, d.jm);
-  const int last_t = k1 - k0 + 2;  // stage t holds plane kk = k0 - 2 + t
+  const int last_t = k1 - k0 + 2;  // group t holds plane kk = k0 - 2 + t
 
-  // stage t into its slot: t = 0 needs only sm(k0-1), t = 1 sm(k0), diu3,6,9(k0), diu7,8(k0-1)
+  // group t: t = 0 needs only sm(k0-1), t = 1 sm(k0), diu3,6,9(k0), diu7,8(k0-1)
   auto issue = [&](int t) {  // by the 32 lanes of warp 0
     const int q = t % NS, kk = k0 - 2 + t;
     const uint32_t mask = (t == 0) ? 0x1u : (t == 1) ? 0x3c9u : 0xffffu;  // maps issued
@@ -1043,10 +1044,15 @@ __global__ void __launch_bounds__(VTX *VTY, 2) k_les_visc_tma(LesDom d, const __
     __syncwarp();
     if (tx < NMAP && ((mask >> tx) & 1u)) {
       if (tx < 10) {
-        const int z = (tx == 0 || tx == 3 || tx == 6 || tx == 9) ? kk + 1 : kk;
-        tma_load_3d(S.st[q].h[tx], &M.m[tx], i0, j0 + LES_JOFF, z + LES_KOFF, &S.bar[q]);
+        float *dst;
+        int z = kk;
+        if (tx == 0) { dst = S.sm[t % NS]; z = kk + 1; }
+        else if (tx == 3 || tx == 6 || tx == 9) { dst = S.z[tx / 3 - 1][t % NZ]; z = kk + 1; }
+        else if (tx == 7 || tx == 8) dst = S.z[tx - 4][t % NZ];
+        else dst = S.x[tx == 1 ? 0 : tx == 2 ? 1 : tx == 4 ? 2 : 3][t % NX1];
+        tma_load_3d(dst, &M.m[tx], i0, j0 + LES_JOFF, z + LES_KOFF, &S.bar[q]);
       } else {
-        tma_load_3d(S.st[q].c[tx - 10], &M.m[tx], i0 + 1 + LES_IOFF, j0 + 1 + LES_JOFF, kk + LES_KOFF, &S.bar[q]);
+        tma_load_3d(S.c[tx - 10][t % NX1], &M.m[tx], i0 + 1 + LES_IOFF, j0 + 1 + LES_JOFF, kk + LES_KOFF, &S.bar[q]);
       }
     }
   };
@@ -1065,7 +1071,7 @@ __global__ void __launch_bounds__(VTX *VTY, 2) k_les_visc_tma(LesDom d, const __
   // step's results are void and reported) so the march still ends in bounded time
   bool bad = false;
   int waited = -1;
-  auto wait_stage = [&](int t) {
+  auto wait_group = [&](int t) {
     if (bad) return;
     if (mbar_wait(&S.bar[t % NS], (uint32_t)((t / NS) & 1))) {
       waited = t;
@@ -1081,45 +1087,52 @@ __global__ void __launch_bounds__(VTX *VTY, 2) k_les_visc_tma(LesDom d, const __
     rv = __ldg(&d.rvspd[(jc + LES_JOFF) * d.pi + ic + LES_IOFF]);
   }
   int c = lix(d, ic, jc, k0);
-  wait_stage(0);
-  wait_stage(1);
+  wait_group(0);
+  wait_group(1);
   const int o = (ty + 1) * VBW + tx + 4;  // this cell in a halo box
   const int oc = ty * VTX + tx;           // and in a cell box
   for (int k = k0; k <= k1; ++k) {
     const int t = k - k0 + 2;
-    wait_stage(t);
-    const ViscStage &A = S.st[t % NS], &B = S.st[(t - 1) % NS], &C = S.st[(t - 2) % NS];
-#define HA(q, da, db) A.h[q][o + (db) * VBW + (da)]
-#define HB(q, da, db) B.h[q][o + (db) * VBW + (da)]
-#define HC(q, da, db) C.h[q][o + (db) * VBW + (da)]
+    wait_group(t);
+    const float *smA = S.sm[t % NS], *smB = S.sm[(t - 1) % NS], *smC = S.sm[(t - 2) % NS];
+    const int za = t % NZ, zb = (t - 1) % NZ, xa = t % NX1;
+#define SA(da, db) smA[o + (db) * VBW + (da)]
+#define SB(da, db) smB[o + (db) * VBW + (da)]
+#define SC(da, db) smC[o + (db) * VBW + (da)]
+#define ZA(n, da, db) S.z[n][za][o + (db) * VBW + (da)]
+#define ZB(n, da, db) S.z[n][zb][o + (db) * VBW + (da)]
+#define XA(n, da, db) S.x[n][xa][o + (db) * VBW + (da)]
     ViscIn v;
-    v.s_c = HB(0, 0, 0); v.s_e = HB(0, 1, 0); v.s_w = HB(0, -1, 0);
-    v.s_n = HB(0, 0, 1); v.s_s = HB(0, 0, -1);
-    v.s_ne = HB(0, 1, 1); v.s_se = HB(0, 1, -1); v.s_nw = HB(0, -1, 1);
-    v.s_u = HA(0, 0, 0); v.s_eu = HA(0, 1, 0); v.s_wu = HA(0, -1, 0);
-    v.s_nu = HA(0, 0, 1); v.s_su = HA(0, 0, -1);
-    v.s_d = HC(0, 0, 0); v.s_ed = HC(0, 1, 0);
-    v.g1c = HA(1, 0, 0); v.g1e = HA(1, 1, 0);
-    v.g2c = HA(2, 0, 0); v.g2n = HA(2, 0, 1); v.g2wn = HA(2, -1, 1);
-    v.g3c = HB(3, 0, 0); v.g3u = HA(3, 0, 0); v.g3wu = HA(3, -1, 0);
-    v.g4c = HA(4, 0, 0); v.g4e = HA(4, 1, 0); v.g4es = HA(4, 1, -1);
-    v.g5c = HA(5, 0, 0); v.g5n = HA(5, 0, 1);
-    v.g6c = HB(6, 0, 0); v.g6u = HA(6, 0, 0); v.g6su = HA(6, 0, -1);
-    v.g7c = HA(7, 0, 0); v.g7e = HA(7, 1, 0); v.g7ed = HB(7, 1, 0);
-    v.g8c = HA(8, 0, 0); v.g8n = HA(8, 0, 1); v.g8nd = HB(8, 0, 1);
-    v.g9c = HB(9, 0, 0); v.g9u = HA(9, 0, 0);
-#undef HA
-#undef HB
-#undef HC
-    v.f0 = A.c[0][oc]; v.g0 = A.c[1][oc]; v.h0 = A.c[2][oc];
+    v.s_c = SB(0, 0); v.s_e = SB(1, 0); v.s_w = SB(-1, 0);
+    v.s_n = SB(0, 1); v.s_s = SB(0, -1);
+    v.s_ne = SB(1, 1); v.s_se = SB(1, -1); v.s_nw = SB(-1, 1);
+    v.s_u = SA(0, 0); v.s_eu = SA(1, 0); v.s_wu = SA(-1, 0);
+    v.s_nu = SA(0, 1); v.s_su = SA(0, -1);
+    v.s_d = SC(0, 0); v.s_ed = SC(1, 0);
+    v.g1c = XA(0, 0, 0); v.g1e = XA(0, 1, 0);
+    v.g2c = XA(1, 0, 0); v.g2n = XA(1, 0, 1); v.g2wn = XA(1, -1, 1);
+    v.g3c = ZB(0, 0, 0); v.g3u = ZA(0, 0, 0); v.g3wu = ZA(0, -1, 0);
+    v.g4c = XA(2, 0, 0); v.g4e = XA(2, 1, 0); v.g4es = XA(2, 1, -1);
+    v.g5c = XA(3, 0, 0); v.g5n = XA(3, 0, 1);
+    v.g6c = ZB(1, 0, 0); v.g6u = ZA(1, 0, 0); v.g6su = ZA(1, 0, -1);
+    v.g7c = ZA(3, 0, 0); v.g7e = ZA(3, 1, 0); v.g7ed = ZB(3, 1, 0);
+    v.g8c = ZA(4, 0, 0); v.g8n = ZA(4, 0, 1); v.g8nd = ZB(4, 0, 1);
+    v.g9c = ZB(2, 0, 0); v.g9u = ZA(2, 0, 0);
+#undef SA
+#undef SB
+#undef SC
+#undef ZA
+#undef ZB
+#undef XA
+    v.f0 = S.c[0][xa][oc]; v.g0 = S.c[1][xa][oc]; v.h0 = S.c[2][xa][oc];
     float fo = 0.f, go = 0.f, ho = 0.f;
-    if (AD) { fo = A.c[3][oc]; go = A.c[4][oc]; ho = A.c[5][oc]; }
+    if (AD) { fo = S.c[3][xa][oc]; go = S.c[4][xa][oc]; ho = S.c[5][xa][oc]; }
     v.ru = ru; v.rv = rv;
     float fv, gv, hv;
     unsigned bd = 0;
     visc_compute<P2, ZF>(d, v, cc, visc_z(d, k), k, fv, gv, hv, bd);
-    // every thread is done with stage t-2: its slot takes stage t+1+VLA; a plane with a
-    // deferred cell is stored by the fixup
+    // every thread is done with this step's reads: group t+1+VLA may take the slots they
+    // used; a plane with a deferred cell is stored by the fixup
     const bool defer = ZF && __syncthreads_or(in ? bd : 0u);
     if (!ZF) __syncthreads();
     if (ty == 0) {  // warp 0 (uniform: issue holds a __syncwarp); none of it issues after a failed wait
