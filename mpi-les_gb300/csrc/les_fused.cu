@@ -956,9 +956,9 @@ __global__ void __launch_bounds__(VTX *VTY) k_les_visc_fix(LesDom d, uint3 g) {
 
 // ---- the halo entries of diu that les reads through index remaps ----------------------
 // The copies vel2.f95:202-318 makes, written into the stored arrays after velfg (and its
-// fixup) so that the TMA-fed march reads plain boxes: diu1, diu4, diu7 at i = im+1 (the
+// fixup) so that the TMA-fed sm pass and viscous march read plain boxes: diu1, diu4, diu7 at i = im+1 (the
 // values at i = im), diu2, diu5, diu8 at j = jm+1 (at j = 1), diu4 at j = 0 (at j = jm)
-// for k = 1..km, diu6 at j = 0 for k = 2..km+1, and diu4 at (im+1, 0) (at (im, jm)).  The
+// for k = 1..km, diu6 at j = 0 for k = 1..km+1, and diu4 at (im+1, 0) (at (im, jm)).  The
 // other remapped entries read as zero (diu2, diu3 at i = 0; diu7, diu8 at k = 0; diu9 at
 // k = km+1): nothing writes them, and the arrays start zeroed.  One thread per face
 // point (jm of the i face, im of the j faces, the corner), one block row per plane.
@@ -982,14 +982,123 @@ __global__ void k_diu_halo(LesDom d) {
       const int cm = lix(d, i, d.jm, k);
       d.diu[4][cm - jmp] = d.diu[4][cm];
     }
-    if (k >= 2) {
-      const int cm = lix(d, i, d.jm, k);
-      d.diu[6][cm - jmp] = d.diu[6][cm];
-    }
+    const int cm = lix(d, i, d.jm, k);
+    d.diu[6][cm - jmp] = d.diu[6][cm];
   } else if (t == d.jm + d.im && k <= d.km) {
     const int c = lix(d, d.im, d.jm, k);
     d.diu[4][c + 1 - jmp] = d.diu[4][c];
   }
+}
+
+// halo boxes of the TMA-fed les kernels: 40 x 10 floats (VHB), slots VHS floats apart
+// (a 128-byte multiple); cell boxes 32 x 8 (VCB)
+constexpr int VBW = 40, VHB = VBW * VTH, VHS = 416, VCB = VTX * VTY;
+
+// ---- sm from TMA-staged diu planes ---------------------------------------------------
+// k_les_sm3's arithmetic (les.f95:45-65) on 32 x 8 column tiles marching k, with the diu
+// planes it reads brought by tensor copies (40 x 10 boxes, as the viscous march below
+// reads them; k_diu_halo has stored the remapped halo entries).  Copy group kk brings
+// diu1,2,4,5,9,7,8 at kk and diu3,6 at kk+1; step k reads groups k and k-1 (diu3,6 at
+// k and k+1, diu7,8 at k-1 and k).  Rings: diu3,6,7,8 2+VLA planes, the rest 1+VLA;
+// once every thread has finished step k the group of plane k+1+VLA is issued.
+template <int VLA>
+struct SmSmem {
+  float z[4][2 + VLA][VHS];  // diu3, diu6 (at kk+1), diu7, diu8 (at kk)
+  float x[5][1 + VLA][VHS];  // diu1, diu2, diu4, diu5, diu9 (at kk)
+  uint64_t bar[2 + VLA];
+};
+struct LesSmMaps {
+  CUtensorMap m[9];  // diu1..9
+};
+
+template <int VLA>
+__global__ void __launch_bounds__(VTX *VTY) k_les_sm_tma(LesDom d, const __grid_constant__ LesSmMaps M, int kchunk) {
+  extern __shared__ __align__(1024) unsigned char ssm_raw[];
+  constexpr int NB = 2 + VLA, NZ = 2 + VLA, NX1 = 1 + VLA;
+  SmSmem<VLA> &S = *reinterpret_cast<SmSmem<VLA> *>(ssm_raw);
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * VTX + tx;
+  const int i0 = blockIdx.x * VTX, j0 = blockIdx.y * VTY;
+  const int k0 = blockIdx.z * kchunk + 1, k1 = min(k0 + kchunk - 1, d.km);
+  const int i = i0 + tx + 1, j = j0 + ty + 1;
+  const bool in = (i <= d.im && j <= d.jm);
+  const int last_t = k1 - k0 + 1;  // group t holds plane kk = k0 - 1 + t
+  // diu_n of the box lanes issue: lane q < 9 copies diu(q+1); group 0 needs diu3, 6, 7, 8 only
+  auto issue = [&](int t) {  // by the 32 lanes of warp 0
+    const int q = t % NB, kk = k0 - 1 + t;
+    const uint32_t bytes = (t == 0 ? 4u : 9u) * VHB * 4u;
+    if (tx == 0) mbar_expect_tx(&S.bar[q], bytes);
+    __syncwarp();
+    const int n = tx + 1;
+    if (tx < 9 && (t > 0 || n == 3 || n == 6 || n == 7 || n == 8)) {
+      float *dst;
+      int z = kk;
+      if (n == 3 || n == 6) { dst = S.z[n / 3 - 1][t % NZ]; z = kk + 1; }
+      else if (n == 7 || n == 8) dst = S.z[n - 5][t % NZ];
+      else dst = S.x[n == 1 ? 0 : n == 2 ? 1 : n == 4 ? 2 : n == 5 ? 3 : 4][t % NX1];
+      tma_load_3d(dst, &M.m[tx], i0, j0 + LES_JOFF, z + LES_KOFF, &S.bar[q]);
+    }
+  };
+  if (tid == 0) {
+    for (int q = 0; q < NB; ++q) mbar_init(&S.bar[q], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  int issued = -1;
+  if (ty == 0)
+    for (int t = 0; t < NB && t <= last_t; ++t) {
+      issue(t);
+      issued = t;
+    }
+  bool bad = false;
+  int waited = -1;
+  auto wait_group = [&](int t) {
+    if (bad) return;
+    if (mbar_wait(&S.bar[t % NB], (uint32_t)((t / NB) & 1))) {
+      waited = t;
+    } else {
+      bad = true;
+      d.ctl[CT_ERROR] = 1;
+    }
+  };
+  wait_group(0);
+  const int o = (ty + 1) * VBW + tx + 4;  // this cell in a halo box
+  int c = lix(d, min(i, d.im), min(j, d.jm), k0);
+  for (int k = k0; k <= k1; ++k) {
+    const int t = k - k0 + 1;
+    wait_group(t);
+    const int za = t % NZ, zb = (t - 1) % NZ, xa = t % NX1;
+#define ZA(n, da, db) S.z[n][za][o + (db) * VBW + (da)]
+#define ZB(n, da, db) S.z[n][zb][o + (db) * VBW + (da)]
+#define XA(n, da, db) S.x[n][xa][o + (db) * VBW + (da)]
+    const float dudxx1 = XA(0, 0, 0);
+    const float dudyx1 = (XA(1, -1, 0) + XA(1, -1, 1) + XA(1, 0, 0) + XA(1, 0, 1)) * .25f;
+    const float dudzx1 = (ZB(0, -1, 0) + ZA(0, -1, 0) + ZB(0, 0, 0) + ZA(0, 0, 0)) * .25f;
+    const float dvdxx1 = (XA(2, 0, 0) + XA(2, 0, -1) + XA(2, 1, 0) + XA(2, 1, -1)) * .25f;
+    const float dvdyx1 = XA(3, 0, 0);
+    const float dvdzx1 = (ZB(1, 0, -1) + ZA(1, 0, -1) + ZB(1, 0, 0) + ZA(1, 0, 0)) * .25f;
+    const float dwdxx1 = (ZA(2, 0, 0) + ZB(2, 0, 0) + ZA(2, 1, 0) + ZB(2, 1, 0)) * .25f;
+    const float dwdyx1 = (ZA(3, 0, 0) + ZB(3, 0, 0) + ZA(3, 0, 1) + ZB(3, 0, 1)) * .25f;
+    const float dwdzx1 = XA(4, 0, 0);
+#undef ZA
+#undef ZB
+#undef XA
+    const float cd = 0.1f * d.gr.delx1[k];
+    const float s1 = dudyx1 + dvdxx1, s2 = dwdyx1 + dvdzx1, s3 = dudzx1 + dwdxx1;
+    const float smv =
+        cd * cd * __fsqrt_rn(2.f * (dudxx1 * dudxx1 + dvdyx1 * dvdyx1 + dwdzx1 * dwdzx1) + s1 * s1 + s2 * s2 + s3 * s3);
+    __syncthreads();  // every thread has read step k: group k+1+VLA may take the slots of k-1 and k
+    if (ty == 0) {    // warp 0 (uniform: issue holds a __syncwarp); none of it issues after a failed wait
+      const bool wbad = __any_sync(0xffffffffu, bad);
+      if (!wbad && t + 1 + VLA <= last_t) {
+        issue(t + 1 + VLA);
+        issued = t + 1 + VLA;
+      }
+    }
+    if (in) d.sm[c] = smv;
+    c += d.np;
+  }
+  if (ty == 0 && bad)
+    for (int t = waited + 1; t <= issued; ++t) (void)mbar_wait(&S.bar[t % NB], (uint32_t)((t / NB) & 1));
 }
 
 // ---- the TMA-fed viscous march -------------------------------------------------------
@@ -1008,7 +1117,6 @@ __global__ void k_diu_halo(LesDom d) {
 // per lane) after lane 0 has armed the group's mbarrier with the bytes to expect; every
 // thread waits (bounded) for the groups it reads.  The arithmetic is visc_compute's,
 // so the fields are bitwise those of k_les_visc_march.
-constexpr int VBW = 40, VHB = VBW * VTH, VHS = 416, VCB = VTX * VTY;  // VHS: slot stride (128-byte multiple)
 struct LesViscMaps {
   CUtensorMap m[16];  // sm, diu1..9, f, g, h, fold, gold, hold
 };
@@ -1229,6 +1337,7 @@ struct ViscF {
   static constexpr auto fn = k_les_visc_fix<A, C>;
 };
 constexpr int kViscLookahead = 1;  // stages in flight beyond the three a step reads
+constexpr int kSmLookahead = 1;    // copy groups in flight beyond the two a step of the sm pass reads
 template <bool A, bool B, bool C>
 struct ViscTmaK {
   static constexpr auto fn = k_les_visc_tma<A, B, C, kViscLookahead>;
@@ -1283,7 +1392,27 @@ void les_launch_velfg_fused(const LesDom &d, bool with_feedbf, LesCtx ctx) {
 }
 
 void les_launch_les_fused(const LesDom &d, bool with_adam, LesCtx ctx) {
-  {  // sm: chunks of planes enough for about sixteen blocks per SM, 8 to 32 planes each
+  static const int kind = [] {  // LES_VISC_KIND=0: the register-staged sm pass and march (A/B measurements)
+    const char *e = getenv("LES_VISC_KIND");
+    return e ? atoi(e) : 1;
+  }();
+  LesViscMaps maps;
+  const bool tma = kind != 0 && (d.pi * 4) % 16 == 0 && visc_maps(d, &maps);
+  if (tma) {
+    // the diu halo entries the TMA boxes read, then sm from the staged diu planes
+    LAUNCH(ctx, (k_diu_halo<<<dim3((d.im + d.jm + 1 + 255) / 256, d.km + 1), 256, 0, ctx.s>>>(d)));
+    LesSmMaps sm_maps;
+    for (int q = 0; q < 9; ++q) sm_maps.m[q] = maps.m[q + 1];
+    static const int kc_env = [] {  // LES_SM_KCHUNK: planes per CTA of the sm pass (A/B measurements)
+      const char *e = getenv("LES_SM_KCHUNK");
+      return e ? atoi(e) : 0;
+    }();
+    const int kc = std::max(1, std::min(d.km, kc_env > 0 ? kc_env : 15));  // 15 to 30 planes measured alike
+    const size_t bytes = sizeof(SmSmem<kSmLookahead>);
+    cudaFuncSetAttribute(k_les_sm_tma<kSmLookahead>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    const dim3 g((d.im + VTX - 1) / VTX, (d.jm + VTY - 1) / VTY, (d.km + kc - 1) / kc);
+    LAUNCH(ctx, (k_les_sm_tma<kSmLookahead><<<g, dim3(VTX, VTY), bytes, ctx.s>>>(d, sm_maps, kc)));
+  } else {  // sm: chunks of planes enough for about sixteen blocks per SM, 8 to 32 planes each
     const long long tiles = (long long)((d.im + STX - 1) / STX) * ((d.jm + STY - 1) / STY);
     const int sms = d.sms > 0 ? d.sms : 152;
     const int nch = (int)std::max<long long>(1, (16LL * sms + tiles - 1) / tiles);
@@ -1295,12 +1424,7 @@ void les_launch_les_fused(const LesDom &d, bool with_adam, LesCtx ctx) {
   // the k-march: 32 x 8 column tiles, chunks of VKC planes; TMA-fed when the arrays'
   // tensor maps could be made (row pitch a multiple of 16 bytes), else register-staged
   const dim3 gv((d.im + VTX - 1) / VTX, (d.jm + VTY - 1) / VTY, (d.km + VKC - 1) / VKC);
-  static const int kind = [] {  // LES_VISC_KIND=0: the register-staged march (A/B measurements)
-    const char *e = getenv("LES_VISC_KIND");
-    return e ? atoi(e) : 1;
-  }();
-  LesViscMaps maps;
-  if (kind != 0 && (d.pi * 4) % 16 == 0 && visc_maps(d, &maps)) {
+  if (tma) {
     const size_t bytes = sizeof(ViscSmem<kViscLookahead>);
     const int v = (d.xy_pow2 ? 4 : 0) | (d.zfast ? 2 : 0) | (with_adam ? 1 : 0);
     auto set_attr = [&](const void *fn) {
@@ -1316,7 +1440,6 @@ void les_launch_les_fused(const LesDom &d, bool with_adam, LesCtx ctx) {
       case 6: set_attr((const void *)ViscTmaK<true, true, false>::fn); break;
       default: set_attr((const void *)ViscTmaK<true, true, true>::fn); break;
     }
-    LAUNCH(ctx, (k_diu_halo<<<dim3((d.im + d.jm + 1 + 255) / 256, d.km + 1), 256, 0, ctx.s>>>(d)));
     launch_variant_smem<ViscTmaK, ViscF>(d, with_adam, ctx, gv, dim3(VTX, VTY), bytes, maps);
     return;
   }
