@@ -205,26 +205,41 @@ __global__ void __launch_bounds__(BX *BY) k_feedbf(LesDom d) {
 }
 
 // boundsm.f95:18-64, three ordered phases
-__global__ void k_boundsm_i(LesDom d) {  // j = -1..jm+1, k = 0..km+1
-  const int j = blockIdx.x * blockDim.x + threadIdx.x - 1;
-  const int k = blockIdx.y;
-  if (j > d.jm + 1) return;
-  d.sm[lix(d, 0, j, k)] = d.sm[lix(d, 1, j, k)];
-  d.sm[lix(d, d.im + 1, j, k)] = d.sm[lix(d, d.im, j, k)];
-}
-__global__ void k_boundsm_j(LesDom d) {  // i = 0..im+1, k = 0..km+1
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int k = blockIdx.y;
-  if (i > d.im + 1) return;
-  d.sm[lix(d, i, d.jm + 1, k)] = d.sm[lix(d, i, d.jm, k)];
-  d.sm[lix(d, i, 0, k)] = d.sm[lix(d, i, 1, k)];
-}
-__global__ void k_boundsm_k(LesDom d) {  // i = 0..im+1, j = -1..jm+1
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y - 1;
-  if (i > d.im + 1) return;
-  d.sm[lix(d, i, j, 0)] = -d.sm[lix(d, i, j, 1)];
-  d.sm[lix(d, i, j, d.km + 1)] = d.sm[lix(d, i, j, d.km)];
+// boundsm.f95:5-69 as one pass.  The reference's three passes (i halos for j = -1..jm+1,
+// then j halos 0 and jm+1 for i = 0..im+1, then k halos 0 (negated) and km+1 for i =
+// 0..im+1, j = -1..jm+1, each reading what the one before wrote) compose to: a halo
+// point takes the value at its source point, clamped into i = 1..im, j = 1..jm (row
+// j = -1 stays -1: no pass writes it for i = 1..im) and k = 1..km, negated on k = 0.
+// No source point is a halo point this kernel writes, so the points are independent.
+// One thread per point of the k faces (k = 0, km+1: (im+2) x (jm+3) each), the i faces
+// (i = 0, im+1; j = -1..jm+1; k = 1..km) and the j faces (j = 0, jm+1; i = 1..im;
+// k = 1..km).
+__global__ void k_boundsm_all(LesDom d) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long nk = (long long)(d.im + 2) * (d.jm + 3), ni = (long long)(d.jm + 3) * d.km,
+                  nj = (long long)d.im * d.km;
+  int i, j, k;
+  if (t < 2 * nk) {
+    const long long r = t % nk;
+    k = (t < nk) ? 0 : d.km + 1;
+    i = (int)(r % (d.im + 2));
+    j = (int)(r / (d.im + 2)) - 1;
+  } else if (t < 2 * nk + 2 * ni) {
+    const long long u = t - 2 * nk, r = u % ni;
+    i = (u < ni) ? 0 : d.im + 1;
+    j = (int)(r % (d.jm + 3)) - 1;
+    k = (int)(r / (d.jm + 3)) + 1;
+  } else if (t < 2 * nk + 2 * ni + 2 * nj) {
+    const long long u = t - 2 * nk - 2 * ni, r = u % nj;
+    j = (u < nj) ? 0 : d.jm + 1;
+    i = (int)(r % d.im) + 1;
+    k = (int)(r / d.im) + 1;
+  } else {
+    return;
+  }
+  const int is = min(max(i, 1), d.im), js = (j == -1) ? -1 : min(max(j, 1), d.jm), ks = min(max(k, 1), d.km);
+  const float v = d.sm[lix(d, is, js, ks)];
+  d.sm[lix(d, i, j, k)] = (k == 0) ? -v : v;
 }
 
 // ------------------------------------------------------------------ adam.f95:30-44
@@ -490,6 +505,39 @@ __global__ void k_boundp1_j(LesDom d, int obey) {
   d.p[lix(d, i, 0, k)] = d.p[lix(d, i, d.jm, k)];
   d.p[lix(d, i, d.jm + 1, k)] = d.p[lix(d, i, 1, k)];
 }
+// boundp1 then boundp2 as one pass (the end of press): the i halos (Neumann) for j =
+// 0..jm+1, then the periodic j halos for i = 0..im+1, then the k halos (Neumann) for
+// i = 0..im+1, j = 0..jm+1, each reading what the one before wrote, compose to: a halo
+// point takes the value at its source point, i clamped into 1..im, j = 0 -> jm and
+// jm+1 -> 1, k clamped into 1..km.  No source point is a halo point, so the points are
+// independent.  One thread per point of the k faces ((im+2) x (jm+2) each), the i faces
+// (j = 0..jm+1, k = 1..km) and the j faces (i = 1..im, k = 1..km).
+__global__ void k_boundp_all(LesDom d) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long nk = (long long)(d.im + 2) * (d.jm + 2), ni = (long long)(d.jm + 2) * d.km,
+                  nj = (long long)d.im * d.km;
+  int i, j, k;
+  if (t < 2 * nk) {
+    const long long r = t % nk;
+    k = (t < nk) ? 0 : d.km + 1;
+    i = (int)(r % (d.im + 2));
+    j = (int)(r / (d.im + 2));
+  } else if (t < 2 * nk + 2 * ni) {
+    const long long u = t - 2 * nk, r = u % ni;
+    i = (u < ni) ? 0 : d.im + 1;
+    j = (int)(r % (d.jm + 2));
+    k = (int)(r / (d.jm + 2)) + 1;
+  } else if (t < 2 * nk + 2 * ni + 2 * nj) {
+    const long long u = t - 2 * nk - 2 * ni, r = u % nj;
+    j = (u < nj) ? 0 : d.jm + 1;
+    i = (int)(r % d.im) + 1;
+    k = (int)(r / d.im) + 1;
+  } else {
+    return;
+  }
+  const int is = min(max(i, 1), d.im), js = (j == 0) ? d.jm : (j == d.jm + 1) ? 1 : j, ks = min(max(k, 1), d.km);
+  d.p[lix(d, i, j, k)] = d.p[lix(d, is, js, ks)];
+}
 // boundp2: k halos for i = 0..im+1, j = 0..jm+1 (boundp.f95:16-21)
 __global__ void k_boundp2(LesDom d, int obey) {
   if (obey && d.ctl[CT_CONVERGED]) return;
@@ -610,9 +658,8 @@ void les_launch_feedbf(const LesDom &d, LesCtx ctx) {
 }
 
 void les_launch_boundsm(const LesDom &d, LesCtx ctx) {
-  LAUNCH(ctx, k_boundsm_i<<<dim3((d.jm + 3 + 127) / 128, d.km + 2), 128, 0, ctx.s>>>(d));
-  LAUNCH(ctx, k_boundsm_j<<<dim3((d.im + 2 + 127) / 128, d.km + 2), 128, 0, ctx.s>>>(d));
-  LAUNCH(ctx, k_boundsm_k<<<dim3((d.im + 2 + 127) / 128, d.jm + 3), 128, 0, ctx.s>>>(d));
+  const long long n = 2LL * (d.im + 2) * (d.jm + 3) + 2LL * (d.jm + 3) * d.km + 2LL * d.im * d.km;
+  LAUNCH(ctx, k_boundsm_all<<<(unsigned)((n + 255) / 256), 256, 0, ctx.s>>>(d));
 }
 
 void les_launch_adam(const LesDom &d, LesCtx ctx) {
@@ -685,8 +732,8 @@ void les_launch_pav_adjust(const LesDom &d, LesCtx ctx) {
   LAUNCH(ctx, k_pav_part<<<gr, dim3(BX, BY), 0, ctx.s>>>(d));
   LAUNCH(ctx, k_finish_mean<<<FIN_BLOCKS, FIN_THREADS, 0, ctx.s>>>(d, nb, SC_PAV));
   LAUNCH(ctx, k_sub_mean<<<sub_mean_blocks(d), 32 * SUB_ROWS, 0, ctx.s>>>(d, d.p, SC_PAV));
-  les_launch_boundp1(d, ctx, 0);
-  les_launch_boundp2(d, ctx, 0);
+  const long long n = 2LL * (d.im + 2) * (d.jm + 2) + 2LL * (d.jm + 2) * d.km + 2LL * d.im * d.km;
+  LAUNCH(ctx, k_boundp_all<<<(unsigned)((n + 255) / 256), 256, 0, ctx.s>>>(d));  // boundp1, boundp2
 }
 
 void les_launch_count_nonfinite(const LesDom &d, unsigned long long *bad, LesCtx ctx) {
