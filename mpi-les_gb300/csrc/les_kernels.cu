@@ -100,7 +100,11 @@ __global__ void __launch_bounds__(BX *BY) k_bondv1_fill(LesDom d) {
 // u(im, j, k) are one per row, so many blocks gather them; each block's max and min go
 // to part[], and the last block to finish combines them, all its threads at once (max
 // and min are exact in any order).
+// With INFLOW the same grid-stride loop also writes the inflow planes i = 0, 1 of
+// k_bondv1_inflow (it reads only i = im >= 3, so the two are independent); a step with
+// the n = 1 fill (which reads i = 1 and writes up to im) keeps them apart.
 constexpr int UOUT_BLOCKS = 64, UOUT_THREADS = 256;
+template <bool INFLOW>
 __global__ void __launch_bounds__(UOUT_THREADS) k_bondv1_uout(LesDom d) {
   __shared__ float smax[UOUT_THREADS / 32], smin[UOUT_THREADS / 32];
   __shared__ int last;
@@ -108,6 +112,13 @@ __global__ void __launch_bounds__(UOUT_THREADS) k_bondv1_uout(LesDom d) {
   const int n = d.jm * d.km;
   for (int q = blockIdx.x * UOUT_THREADS + threadIdx.x; q < n; q += gridDim.x * UOUT_THREADS) {
     const int j = q % d.jm + 1, k = q / d.jm + 1;
+    if (INFLOW) {
+      const float a = d.uin[q], b = d.vin[q], c = d.win[q];
+      for (int i = 0; i <= 1; ++i) {
+        const int x = lix(d, i, j, k);
+        d.u[x] = a; d.v[x] = b; d.w[x] = c;
+      }
+    }
     const float x = U_(d.im, j, k);
     aaa = fmaxf(aaa, x);
     bbb = fminf(bbb, x);
@@ -161,28 +172,37 @@ __global__ void k_bondv1_outflow(LesDom d) {
   d.v[c2] = d.v[c2] - d.dt * uout * (d.v[c2] - d.v[c]) / rdx;
   d.w[c2] = d.w[c2] - d.dt * uout * (d.w[c2] - d.w[c]) / rdx;
 }
-// periodic side flow, k = 0..km+1 (w: 0..km), i = 0..im+1 (bondv1.f95:210-229)
-__global__ void k_bondv1_periodic(LesDom d) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int k = blockIdx.y;
-  if (i > d.im + 1) return;
-  const int r0 = lix(d, i, 0, k), rj = lix(d, i, d.jm, k), r1 = lix(d, i, 1, k), rj1 = lix(d, i, d.jm + 1, k);
-  d.u[r0] = d.u[rj]; d.u[rj1] = d.u[r1];
-  d.v[r0] = d.v[rj]; d.v[rj1] = d.v[r1];
-  if (k <= d.km) { d.w[r0] = d.w[rj]; d.w[rj1] = d.w[r1]; }
-}
-// top and underground (bondv1.f95:249-268)
-__global__ void k_bondv1_topbottom(LesDom d) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y - 1;
-  if (i > d.im + 1) return;
-  if (j >= 0) {
-    const int b0 = lix(d, i, j, 0), b1 = lix(d, i, j, 1), tk = lix(d, i, j, d.km), tk1 = lix(d, i, j, d.km + 1);
-    d.u[b0] = -d.u[b1]; d.u[tk1] = d.u[tk];
-    d.v[b0] = -d.v[b1]; d.v[tk1] = d.v[tk];
+// the periodic side flow then the top and underground of bondv1 (bondv1.f95:210-268) as
+// one pass.  The two passes (j halos 0 and jm+1 of u, v for k = 0..km+1 and of w for
+// k = 0..km, for i = 0..im+1; then u, v k halos for j = 0..jm+1 (negated at k = 0) and
+// w = 0 on k = 0 and k = km for j = -1..jm+1) compose to: u, v at a j-halo row point or
+// a k-halo plane point take the value at the source point (j = 0 -> jm, jm+1 -> 1; k
+// clamped into 1..km), negated on k = 0; w is 0 on k = 0 and km, and its j-halo rows
+// for k = 1..km-1 take the wrapped row's value.  No source point is written here.
+__global__ void k_bondv1_sides(LesDom d) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long ni = d.im + 2;
+  const long long na = 2LL * d.km * ni, nb = 2LL * (d.jm + 2) * ni, nc = 2LL * (d.jm + 3) * ni;
+  if (t < na) {  // u, v (and w for k <= km-1) on the j-halo rows, k = 1..km
+    const long long r = t % (d.km * ni);
+    const int j = (t < d.km * ni) ? 0 : d.jm + 1, i = (int)(r % ni), k = (int)(r / ni) + 1;
+    const int js = (j == 0) ? d.jm : 1;
+    const int c = lix(d, i, j, k), cs = lix(d, i, js, k);
+    d.u[c] = d.u[cs];
+    d.v[c] = d.v[cs];
+    if (k <= d.km - 1) d.w[c] = d.w[cs];
+  } else if (t < na + nb) {  // u, v on the k-halo planes, j = 0..jm+1
+    const long long u = t - na, r = u % ((d.jm + 2) * ni);
+    const int k = (u < (d.jm + 2) * ni) ? 0 : d.km + 1, i = (int)(r % ni), j = (int)(r / ni);
+    const int js = (j == 0) ? d.jm : (j == d.jm + 1) ? 1 : j, ks = (k == 0) ? 1 : d.km;
+    const int c = lix(d, i, j, k), cs = lix(d, i, js, ks);
+    d.u[c] = (k == 0) ? -d.u[cs] : d.u[cs];
+    d.v[c] = (k == 0) ? -d.v[cs] : d.v[cs];
+  } else if (t < na + nb + nc) {  // w = 0 on k = 0 and k = km, j = -1..jm+1
+    const long long u = t - na - nb, r = u % ((d.jm + 3) * ni);
+    const int k = (u < (d.jm + 3) * ni) ? 0 : d.km, i = (int)(r % ni), j = (int)(r / ni) - 1;
+    d.w[lix(d, i, j, k)] = 0.f;
   }
-  d.w[lix(d, i, j, 0)] = 0.f;
-  d.w[lix(d, i, j, d.km)] = 0.f;
 }
 
 // ------------------------------------------------------------------ feedbf.f95:35-61
@@ -642,14 +662,16 @@ static void launch_rhs(const LesDom &d, float *dst, int ghost, LesCtx ctx) {
 }
 
 void les_launch_bondv1(const LesDom &d, int n, LesCtx ctx) {
-  LAUNCH(ctx, k_bondv1_inflow<<<dim3((d.jm + 127) / 128, d.km), 128, 0, ctx.s>>>(d));
   if (n == 1) {
+    LAUNCH(ctx, k_bondv1_inflow<<<dim3((d.jm + 127) / 128, d.km), 128, 0, ctx.s>>>(d));
     LAUNCH(ctx, k_bondv1_fill<<<dim3((d.im - 1 + BX - 1) / BX, (d.jm + BY - 1) / BY, d.km), dim3(BX, BY), 0, ctx.s>>>(d));
+    LAUNCH(ctx, k_bondv1_uout<false><<<UOUT_BLOCKS, UOUT_THREADS, 0, ctx.s>>>(d));
+  } else {
+    LAUNCH(ctx, k_bondv1_uout<true><<<UOUT_BLOCKS, UOUT_THREADS, 0, ctx.s>>>(d));
   }
-  LAUNCH(ctx, k_bondv1_uout<<<UOUT_BLOCKS, UOUT_THREADS, 0, ctx.s>>>(d));
   LAUNCH(ctx, k_bondv1_outflow<<<dim3((d.jm + 127) / 128, d.km), 128, 0, ctx.s>>>(d));
-  LAUNCH(ctx, k_bondv1_periodic<<<dim3((d.im + 2 + 127) / 128, d.km + 2), 128, 0, ctx.s>>>(d));
-  LAUNCH(ctx, k_bondv1_topbottom<<<dim3((d.im + 2 + 127) / 128, d.jm + 3), 128, 0, ctx.s>>>(d));
+  const long long ns = 2LL * (d.im + 2) * (d.km + (d.jm + 2) + (d.jm + 3));
+  LAUNCH(ctx, k_bondv1_sides<<<(unsigned)((ns + 255) / 256), 256, 0, ctx.s>>>(d));
 }
 
 
