@@ -48,22 +48,34 @@ __device__ __forceinline__ void velnw_cell(const LesDom &d, int i, int j, int k,
     wn = d.w[c] + d.dt * (__ldg(d.h + c) - pz);
   }
 }
-// velnw of the block (bx, by, bz); ZF: reciprocal-corrected divisions with blocks that
-// meet a dividend outside their range deferred to k_velnw_fix (les_common.cuh)
+// velnw of the block (bx, by, bz): planes bz*VNK+1 .. bz*VNK+VNK of its columns, all
+// computed before any is stored (each cell reads only its own u, v, w, so the update in
+// place is safe); ZF: reciprocal-corrected divisions with blocks that meet a dividend
+// outside their range deferred to k_velnw_fix (les_common.cuh)
+constexpr int VNK = 4;
 template <bool P2, bool ZF>
 __device__ __forceinline__ void velnw_block(const LesDom &d, int bx, int by, int bz) {
-  const int i0 = bx * BX + threadIdx.x + 1, j0 = by * BY + threadIdx.y + 1, k = bz + 1;
+  const int i0 = bx * BX + threadIdx.x + 1, j0 = by * BY + threadIdx.y + 1, ka = bz * VNK + 1;
   const bool in = (i0 <= d.im && j0 <= d.jm);
   const int i = min(i0, d.im), j = min(j0, d.jm);  // past the edge: the edge cell again, not stored
-  const int c = lix(d, i, j, k);
-  float un = 0.f, vn = 0.f, wn = 0.f;
+  float un[VNK], vn[VNK], wn[VNK];
   unsigned bd = 0;
-  velnw_cell<P2, ZF>(d, i, j, k, c, un, vn, wn, bd);
+#pragma unroll
+  for (int q = 0; q < VNK; ++q) {
+    un[q] = vn[q] = wn[q] = 0.f;
+    if (ka + q <= d.km) velnw_cell<P2, ZF>(d, i, j, ka + q, lix(d, i, j, ka + q), un[q], vn[q], wn[q], bd);
+  }
   if (ZF && defer_block(bd, d.fix[FIX_VELNW])) return;
   if (!in) return;
-  d.u[c] = un;
-  d.v[c] = vn;
-  if (k <= d.km - 1) d.w[c] = wn;
+#pragma unroll
+  for (int q = 0; q < VNK; ++q) {
+    const int k = ka + q;
+    if (k > d.km) break;
+    const int c = lix(d, i, j, k);
+    d.u[c] = un[q];
+    d.v[c] = vn[q];
+    if (k <= d.km - 1) d.w[c] = wn[q];
+  }
 }
 template <bool P2, bool ZF>
 __global__ void __launch_bounds__(BX *BY) k_velnw(LesDom d) {
@@ -642,7 +654,7 @@ void les_launch_feedbfm(uint8_t *mask, const float *zbm, const float *thr, int i
 }
 
 void les_launch_velnw(const LesDom &d, LesCtx ctx) {
-  const dim3 g = interior_grid(d, d.km), b(BX, BY);
+  const dim3 g = interior_grid(d, (d.km + VNK - 1) / VNK), b(BX, BY);
   LAUNCH(ctx, LES_PZ_SWITCH(d, k_velnw, <<<g, b, 0, ctx.s>>>(d)));
   if (d.zfast) {
     if (d.xy_pow2) LAUNCH(ctx, (k_velnw_fix<true><<<fix_grid(d, g), b, 0, ctx.s>>>(d, u3(g))));
