@@ -94,6 +94,17 @@ def test_les(built_lib, shape, spacing):
     _assert_same(gpu, orc, STATE, "les")
 
 
+@pytest.mark.parametrize("shape", [(3, 2, 3), (70, 9, 47)])
+def test_les_small_and_chunked(built_lib, shape):
+    """velfg then les at the smallest domain (one partial 32 x 8 tile, tensor-copy boxes
+    mostly outside the arrays) and at a depth that splits the sm pass and the viscous
+    march into several k chunks, with partial tiles in i and j: bitwise the oracle's."""
+    sc, gpu, orc = _pair(shape)
+    gpu.velfg(); orc.stage(ref.VELFG)
+    gpu.les(); orc.stage(ref.LES)
+    _assert_same(gpu, orc, STATE, f"les {shape}")
+
+
 @pytest.mark.parametrize("shape", SHAPES)
 def test_adam(built_lib, shape):
     sc, gpu, orc = _pair(shape)
