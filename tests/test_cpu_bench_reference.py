@@ -1,7 +1,8 @@
-"""CPU check of bench.py's reference arm (the CPU path the driver times beside the GPU
-arm): one JSON line with the contract's keys, the same metric and workload as the GPU
-line, and a positive throughput, on this machine's cores; the arm loads nothing of the
-GPU product.  Run on a smaller domain of the same kind (--dims) to stay quick here."""
+"""CPU check of bench.py's reference arm (`--impl reference`: the reference's CPU path,
+timed beside the GPU arm): one JSON line with the bench line's keys, the same metric and
+workload as the GPU line, and a positive throughput, on this machine's cores; the arm
+loads nothing of the GPU product.  Run on a smaller domain of the same kind (--dims) to
+stay quick here."""
 import json
 import os
 import subprocess
