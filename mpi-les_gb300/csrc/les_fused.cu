@@ -956,9 +956,10 @@ __global__ void __launch_bounds__(VTX *VTY) k_les_visc_fix(LesDom d, uint3 g) {
 
 // ---- the halo entries of diu that les reads through index remaps ----------------------
 // The copies vel2.f95:202-318 makes, written into the stored arrays after velfg (and its
-// fixup) so that the TMA-fed sm pass and viscous march read plain boxes: diu1, diu4, diu7 at i = im+1 (the
-// values at i = im), diu2, diu5, diu8 at j = jm+1 (at j = 1), diu4 at j = 0 (at j = jm)
-// for k = 1..km, diu6 at j = 0 for k = 1..km+1, and diu4 at (im+1, 0) (at (im, jm)).  The
+// fixup) so that the TMA-fed sm pass and viscous march read plain boxes: diu1, diu4,
+// diu7 at i = im+1 (the values at i = im), diu2, diu5, diu8 at j = jm+1 (at j = 1), diu4
+// at j = 0 (at j = jm) for k = 1..km, diu6 at j = 0 for k = 1..km+1, and diu4 at
+// (im+1, 0) (at (im, jm)).  The
 // other remapped entries read as zero (diu2, diu3 at i = 0; diu7, diu8 at k = 0; diu9 at
 // k = km+1): nothing writes them, and the arrays start zeroed.  One thread per face
 // point (jm of the i face, im of the j faces, the corner), one block row per plane.
@@ -1113,9 +1114,9 @@ __global__ void __launch_bounds__(VTX *VTY) k_les_sm_tma(LesDom d, const __grid_
 // has finished step k the group of plane k+1+VLA is issued, so the copies of VLA steps
 // are in flight while a step computes.  Each array has a ring of its own, as deep as its
 // reach: sm 3+VLA planes (read at k-1, k, k+1), diu3,6,9,7,8 2+VLA (two planes each),
-// diu1,2,4,5 and the cell arrays 1+VLA, so that three CTAs fit an SM's shared memory.  Warp 0 issues a group (one copy
-// per lane) after lane 0 has armed the group's mbarrier with the bytes to expect; every
-// thread waits (bounded) for the groups it reads.  The arithmetic is visc_compute's,
+// diu1,2,4,5 and the cell arrays 1+VLA, so that three CTAs fit an SM's shared memory.
+// Warp 0 issues a group (one copy per lane) after lane 0 has armed the group's mbarrier
+// with the bytes to expect; every thread waits (bounded) for the groups it reads.  The arithmetic is visc_compute's,
 // so the fields are bitwise those of k_les_visc_march.
 struct LesViscMaps {
   CUtensorMap m[16];  // sm, diu1..9, f, g, h, fold, gold, hold
@@ -1343,8 +1344,9 @@ struct ViscTmaK {
   static constexpr auto fn = k_les_visc_tma<A, B, C, kViscLookahead>;
 };
 
-// Tensor maps of the arrays the viscous march reads, cached per domain layout (the
-// maps hold only base addresses, extents and strides).
+// Tensor maps of the arrays the TMA-fed sm pass and viscous march read (sm, diu1..9 as
+// halo boxes, f..hold as cell boxes), cached per domain layout (the maps hold only base
+// addresses, extents and strides).
 bool visc_maps(const LesDom &d, LesViscMaps *out) {
   static std::mutex mu;
   static std::map<std::vector<uintptr_t>, LesViscMaps> cache;
