@@ -97,6 +97,7 @@ struct les_handle {
   float *fscal_d = nullptr;
   unsigned long long *bad_d = nullptr;
   float *sor_d[3] = {};           // internal buffers of the fused SOR sweep (A, B, rhs)
+  float *prow_d = nullptr;        // p's row jm+2 while the fused sweep reads it (LesDom.prow)
   float *diu_d[10] = {};          // diu1..9 stored by velfg for les ([0] unused)
   float *rsp_d = nullptr;         // two planes: u/uspd and v/vspd at k = 1
   unsigned int *cnt_d = nullptr;  // CTA tickets (fused SOR sweep, finish_mean, uout)
@@ -168,7 +169,7 @@ extern "C" size_t les_domain_bytes(int im, int jm, int km) {
   const size_t march = (size_t)((im + 31) / 32) * ((jm + 7) / 8) * km;
   const size_t fix = FIX_COUNT * (2 + std::max({fused, inter, march})) * sizeof(int);
   return (kNumFields + 3 + 9) * field + pi * nj * nk /*mask bytes*/ + 2 * pi * nj * sizeof(float) + part + fix +
-         64 * 1024;
+         (size_t)im * km * sizeof(float) /*p's row jm+2*/ + 64 * 1024;
 }
 
 extern "C" int les_gpu_create(const les_dims *dims, const les_params *params, les_handle **out) {
@@ -212,6 +213,10 @@ extern "C" int les_gpu_create(const les_dims *dims, const les_params *params, le
       return cleanup(LES_ERR_NOMEM);
     }
     cudaMemsetAsync(h->sor_d[q], 0, h->nfloat * sizeof(float), h->s);
+  }
+  if (cudaMalloc(&h->prow_d, (size_t)im * km * sizeof(float)) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return cleanup(LES_ERR_NOMEM);
   }
   for (int q = 1; q <= 9; ++q) {
     if (cudaMalloc(&h->diu_d[q], h->nfloat * sizeof(float)) != cudaSuccess) {
@@ -288,6 +293,7 @@ extern "C" int les_gpu_destroy(les_handle *h) {
   cudaFree(h->fscal_d);
   cudaFree(h->bad_d);
   for (int q = 0; q < 3; ++q) cudaFree(h->sor_d[q]);
+  cudaFree(h->prow_d);
   for (int q = 1; q <= 9; ++q) cudaFree(h->diu_d[q]);
   cudaFree(h->rsp_d);
   cudaFree(h->cnt_d);
@@ -673,7 +679,7 @@ extern "C" int les_gpu_commit_setup(les_handle *h) {
   d.sor_fixed = h->prm.sor_fixed;
   d.sor_ksplit = h->prm.sor_ksplit;
   d.scal = h->scal_d; d.ctl = h->ctl_d; d.part = h->part_d; d.fscal = h->fscal_d;
-  d.sorA = h->sor_d[0]; d.sorB = h->sor_d[1]; d.sorR = h->sor_d[2];
+  d.sorA = h->sor_d[0]; d.sorB = h->sor_d[1]; d.sorR = h->sor_d[2]; d.prow = h->prow_d;
   {  // power-of-two x/y spacings: exact reciprocal multiplications (dvs)
     auto pow2 = [](float x) { int e; return x > 0.f && std::isfinite(x) && std::frexp(x, &e) == 0.5f; };
     const float P = dx1(1), Q = dy1(1);

@@ -74,6 +74,8 @@ struct LesDom {
   float *fscal;    // float copies of uout/rhsav/pav for kernels
   float *sorA, *sorB;  // ping-pong p buffers of the fused SOR sweep (with periodic ghost rows)
   float *sorR;         // rhs of the fused SOR sweep (with periodic ghost rows)
+  float *prow;         // p's row jm+2 (i = 1..im, k = 1..km, i fastest), saved while the
+                       // fused sweep's first iteration reads that row as a ghost copy
   unsigned int *cnt;  // CTA completion tickets: [0] fused SOR sweep, [8] finish_mean, [12] bondv1 uout
   double *part2;      // second-level partial sums of finish_mean (FIN_BLOCKS)
   int sms;         // SMs of the device (grid sizing)

@@ -373,10 +373,17 @@ inline dim3 reduce_grid(const LesDom &d) { return dim3((d.im + BX - 1) / BX, (d.
 // rhs of the cells of block (bx, by, bz) -- columns (i, j), planes bz*RKC+1 .. -- plus
 // its partial of sum(dx1*dy1*dzn*rhs) (press.f95:63-72).  dst: the rhs array (rhs =
 // d.rhs) or the SOR's internal rhs buffer, which also takes periodic ghost copies of
-// rows 1..4 in rows jm+1..jm+4 and of rows jm-3..jm in rows -3..0 (ghost_rows).  ZF: reciprocal-corrected divisions;
+// rows 1..4 in rows jm+1..jm+4 and of rows jm-3..jm in rows -3..0 (ghost_rows).  On that
+// path p takes the same copies, so that the fused sweep's first iteration reads p by
+// tensor copies: rows 0 and jm+1 already hold them (boundp, periodic in j), rows -3..-1
+// and jm+3, jm+4 lie outside p's declared extent, and row jm+2, which lies inside it and
+// which the reference's press never writes, is saved into d.prow first and put back by
+// the sweep's copy-out (rhs reads no p).  ZF: reciprocal-corrected divisions;
 // a block that met a dividend outside their range is recomputed whole by the fixup
 // (rhs only reads u, v, w, f, g, h, so recomputing overwrites with the same cells).
-template <bool P2, bool ZF>
+// PG: also write p's ghost copies (the main kernel; its fixup recomputes deferred blocks'
+// rhs only, the p copies having been written already)
+template <bool P2, bool ZF, bool PG>
 __device__ __forceinline__ void rhs_block(const LesDom &d, float *dst, int ghost, int bx, int by, int bz, uint3 g) {
   const int i0 = bx * BX + threadIdx.x + 1, j0 = by * BY + threadIdx.y + 1;
   const bool in = (i0 <= d.im && j0 <= d.jm);
@@ -395,7 +402,16 @@ __device__ __forceinline__ void rhs_block(const LesDom &d, float *dst, int ghost
     const float rr = rhs_comp<P2, ZF>(d, i, j, k, cur, bd);
     if (in) {
       dst[c] = rr;
-      for_ghost_rows(d.jm, gmask, [&](int off) { dst[c + off * d.pi] = rr; });
+      if (gmask) {
+        const float pv = PG ? d.p[c] : 0.f;
+        for_ghost_rows(d.jm, gmask, [&](int off) {
+          dst[c + off * d.pi] = rr;
+          if (PG) {
+            if (j + off == d.jm + 2) d.prow[(k - 1) * d.im + (i - 1)] = d.p[c + off * d.pi];
+            d.p[c + off * d.pi] = pv;
+          }
+        });
+      }
       acc.add(axy * d.gr.dzn[k] * rr);
     }
     cur = nxt;
@@ -406,11 +422,13 @@ __device__ __forceinline__ void rhs_block(const LesDom &d, float *dst, int ghost
 }
 template <bool P2, bool ZF>
 __global__ void __launch_bounds__(BX *BY) k_rhs(LesDom d, float *dst, int ghost) {
-  rhs_block<P2, ZF>(d, dst, ghost, blockIdx.x, blockIdx.y, blockIdx.z, make_uint3(gridDim.x, gridDim.y, gridDim.z));
+  rhs_block<P2, ZF, true>(d, dst, ghost, blockIdx.x, blockIdx.y, blockIdx.z, make_uint3(gridDim.x, gridDim.y, gridDim.z));
 }
 template <bool P2>
 __global__ void __launch_bounds__(BX *BY) k_rhs_fix(LesDom d, float *dst, int ghost, uint3 g) {
-  for_deferred(d.fix[FIX_RHS], g, [&](int bx, int by, int bz) { rhs_block<P2, false>(d, dst, ghost, bx, by, bz, g); });
+  for_deferred(d.fix[FIX_RHS], g, [&](int bx, int by, int bz) {
+    rhs_block<P2, false, false>(d, dst, ghost, bx, by, bz, g);
+  });
 }
 // pav partials: sum(p*dx1*dy1*dzn) (press.f95:124-133), one per block of RKC planes
 __global__ void __launch_bounds__(BX *BY) k_pav_part(LesDom d) {

@@ -55,13 +55,16 @@ namespace {
 
 // Copy the interior of the buffer the last executed launch wrote back into p, when the
 // sweep stopped before its final (p-writing) launch or ran a single iteration.
-__global__ void k_sor_copyout(LesDom d, int nmaxp) {
-  (void)nmaxp;
-  if (d.ctl[CT_ITERS] < 1 || d.ctl[CT_LASTBUF] == 2) return;  // nothing ran, or p was written
-  const float *src = (d.ctl[CT_LASTBUF] == 1) ? d.sorB : d.sorA;
+__global__ void k_sor_copyout(LesDom d, int restore_prow) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int j = blockIdx.y + 1;
   if (i > d.im) return;
+  // p's row jm+2 as it was before the press (no sweep writes it): plane k by the threads
+  // of row j = 1 + (k-1) mod jm, so the rows share the planes
+  if (restore_prow)
+    for (int k = j; k <= d.km; k += d.jm) d.p[lix(d, i, d.jm + 2, k)] = d.prow[(k - 1) * d.im + (i - 1)];
+  if (d.ctl[CT_ITERS] < 1 || d.ctl[CT_LASTBUF] == 2) return;  // nothing ran, or p was written
+  const float *src = (d.ctl[CT_LASTBUF] == 1) ? d.sorB : d.sorA;
   for (int k = 1; k <= d.km; ++k) {
     const int c = lix(d, i, j, k);
     d.p[c] = src[c];
@@ -148,8 +151,8 @@ int les_tensor_map_3d(CUtensorMap *m, const LesDom &d, const float *base, int bo
 }
 
 int les_sor_make_maps(const LesDom &d, SorShape sh, LesSorMaps *maps) {
-  const float *bases[3] = {d.sorA, d.sorB, d.sorR};
-  for (int q = 0; q < 3; ++q) {
+  const float *bases[4] = {d.sorA, d.sorB, d.sorR, d.p};
+  for (int q = 0; q < 4; ++q) {
     const int rc = les_tensor_map_3d(&maps->m[q], d, bases[q], sh.nx * 4, sh.ny);
     if (rc != 0) return rc;
   }
@@ -167,8 +170,10 @@ void les_launch_sor_iter(const LesDom &d, const SorArgs &a, SorShape sh, const L
   }();
   // the TMA sweep is built for omega = 1 (press.f95:45); another omega takes the register kernel
   const bool tma = kind != 0 && maps && maps->valid && maps->shape.nx == sh.nx && maps->shape.ny == sh.ny &&
-                   cn1mode == 0 && d.omega == 1.f && (a.psrc == d.sorA || a.psrc == d.sorB);
-  const CUtensorMap *tp = tma ? ((a.psrc == d.sorA) ? &maps->m[0] : &maps->m[1]) : nullptr;
+                   cn1mode == 0 && d.omega == 1.f &&
+                   (a.psrc == d.sorA || a.psrc == d.sorB || (a.psrc == d.p && a.src_ghosts && a.depth == 1));
+  const CUtensorMap *tp =
+      tma ? ((a.psrc == d.sorA) ? &maps->m[0] : (a.psrc == d.sorB) ? &maps->m[1] : &maps->m[3]) : nullptr;
   const CUtensorMap *tr = tma ? &maps->m[2] : nullptr;
   if (a.depth == 2) {  // the caller checked les_sor_two_ok
     les_launch_sor_iter2(d, a, sh.ny, *tp, *tr, s);
@@ -205,6 +210,6 @@ void les_launch_sor_redo(const LesDom &d, const SorArgs &two, cudaStream_t s) {
   launch_reg_kc<32, 24, false>(d, a, 0, s);
 }
 
-void les_launch_sor_copyout(const LesDom &d, int nmaxp, cudaStream_t s) {
-  k_sor_copyout<<<dim3((d.im + 127) / 128, d.jm), 128, 0, s>>>(d, nmaxp);
+void les_launch_sor_copyout(const LesDom &d, int restore_prow, cudaStream_t s) {
+  k_sor_copyout<<<dim3((d.im + 127) / 128, d.jm), 128, 0, s>>>(d, restore_prow);
 }

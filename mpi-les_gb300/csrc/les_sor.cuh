@@ -24,6 +24,8 @@ struct SorArgs {
   int redo = 0;          // 1: recompute one iteration only if CT_REDO is set (after a
                          // two-iteration launch whose first iteration met the exit test)
   int dstcode = 0;       // where pdst is, for the copy-out: 0 sorA, 1 sorB, 2 p itself
+  int src_ghosts = 0;    // psrc == p and the SOR-path rhs kernel has just written p's
+                         // periodic ghost rows: the TMA sweep may read p
 };
 
 // Tile shape of the fused sweep: nx float4 columns (32 or 16; the interior i cells per
@@ -35,9 +37,9 @@ struct SorShape {
   int nx = 0, ny = 0, kchunk = 0, depth = 1;
 };
 
-// Tensor maps of the internal buffers (sorA, sorB, sorR) for one tile shape.
+// Tensor maps of the internal buffers (sorA, sorB, sorR) and of p for one tile shape.
 struct LesSorMaps {
-  CUtensorMap m[3];
+  CUtensorMap m[4];
   SorShape shape;
   int valid = 0;
 };
@@ -68,7 +70,8 @@ void les_launch_sor_iter2(const LesDom &d, const SorArgs &a, int ny, const CUten
 // kernel (uniform cn1, one k chunk) otherwise.
 void les_launch_sor_iter_nx16(const LesDom &d, const SorArgs &a, int ny, const CUtensorMap *tp,
                               const CUtensorMap *tr, cudaStream_t s);
-void les_launch_sor_copyout(const LesDom &d, int nmaxp, cudaStream_t s);
+// restore_prow: the press's rhs kernel saved p's row jm+2 (les_kernels.cu): put it back
+void les_launch_sor_copyout(const LesDom &d, int restore_prow, cudaStream_t s);
 // After a two-iteration launch `two` (sor_fixed == 0): recompute its first iteration
 // alone, from the same source into the same destination, if that iteration met the
 // exit test (CT_REDO); otherwise the launch returns at once.

@@ -119,8 +119,12 @@ SorShape les_step_plan_shape(const LesDom &d, LesStepPlan *plan) {
 // iteration.  With the exit test on, each two-iteration launch is followed by a redo
 // launch that cuts it back to its first iteration if that one met the test.
 // ev_first / ev_last (optional) are recorded after the first and after the last launch.
+// p_ghosts: the SOR-path rhs kernel has just written p's periodic ghost rows (saving
+// row jm+2), so the first iteration may read p by tensor copies and the copy-out puts
+// row jm+2 back.
 static void enqueue_sor_fused(const LesDom &d, const les_params &prm, SorShape sh, const LesSorMaps *maps,
-                              LesCtx ctx, cudaEvent_t ev_first = nullptr, cudaEvent_t ev_last = nullptr) {
+                              LesCtx ctx, cudaEvent_t ev_first = nullptr, cudaEvent_t ev_last = nullptr,
+                              bool p_ghosts = false) {
   les_launch_sor_begin(d, ctx);
   const int nit = prm.nmaxp;
   SorShape one = sh;
@@ -149,6 +153,7 @@ static void enqueue_sor_fused(const LesDom &d, const les_params &prm, SorShape s
     a.ntiles = tiles * nchunk;
     a.part = d.part;
     a.counter = d.cnt;
+    a.src_ghosts = (cur == d.p && p_ghosts) ? 1 : 0;
     // a one-iteration launch on a depth-2 plan takes the maps' tile height only if it
     // has a one-iteration kernel (not ny = 32: then the register kernel runs)
     les_launch_sor_iter(d, a, (two || maps == nullptr || maps->shape.ny == one.ny) ? use : one,
@@ -163,7 +168,7 @@ static void enqueue_sor_fused(const LesDom &d, const les_params &prm, SorShape s
     cur = a.pdst;
     l = lend + 1;
   }
-  les_launch_sor_copyout(d, nit, ctx.s);
+  les_launch_sor_copyout(d, p_ghosts ? 1 : 0, ctx.s);
   ++*ctx.nlaunch;
 }
 
@@ -175,7 +180,7 @@ void les_step_enqueue(const LesDom &d, const les_params &prm, SorShape sh, const
   les_launch_bondfg(d, ctx);
   if (sh.ny > 0) {
     les_launch_rhs_sor(d, ctx);
-    enqueue_sor_fused(d, prm, sh, maps, ctx);
+    enqueue_sor_fused(d, prm, sh, maps, ctx, nullptr, nullptr, true);
   } else {
     les_launch_rhs_mean(d, ctx);
     les_launch_sor_simple(d, prm.nmaxp, ctx);
@@ -211,12 +216,13 @@ static void enqueue_part(const LesDom &d, const les_params &prm, SorShape sh, co
     a.ntiles = les_sor_fused_tiles(d.im, d.jm, one) * nchunk;
     a.part = d.part;
     a.counter = d.cnt;
-    les_launch_sor_iter(d, a, one, nullptr, ctx.s);  // reads p: the register kernel
+    a.src_ghosts = 1;  // les_launch_rhs_sor above wrote p's ghost rows
+    const bool fit = maps && maps->valid && maps->shape.nx == one.nx && maps->shape.ny == one.ny;
+    les_launch_sor_iter(d, a, one, fit ? maps : nullptr, ctx.s);
     ++*ctx.nlaunch;
-    (void)maps;
     (void)prm;
   } else {
-    les_launch_sor_copyout(d, prm.nmaxp, ctx.s);
+    les_launch_sor_copyout(d, 1, ctx.s);  // part 1 ran the SOR-path rhs kernel
     ++*ctx.nlaunch;
     les_launch_pav_adjust(d, ctx);
   }
