@@ -82,6 +82,10 @@ module module_LES_gpu
       real(c_float), intent(inout) :: host(*)
       integer(c_int), intent(in) :: lb(3), ub(3)
     end function
+    integer(c_int) function les_gpu_sync(h) bind(C, name='les_gpu_sync')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h
+    end function
     integer(c_int) function les_gpu_download_async(h, field, host, lb, ub, ticket) &
         bind(C, name='les_gpu_download_async')
       import :: c_int, c_ptr, c_float, c_long_long
@@ -334,6 +338,9 @@ contains
     real(4), intent(inout) :: w(0:im+1, -1:jm+1, -1:km+1), p(0:im+2, 0:jm+2, 0:km+1)
     real(4), intent(inout) :: usum(0:im, 0:jm, 0:km), vsum(0:im, 0:jm, 0:km), wsum(0:im, 0:jm, 0:km)
     real(4), intent(inout) :: fold(im, jm, km), gold(im, jm, km), hold(im, jm, km)
+    ! the steps since the last sync finished (a kernel's bounded wait that gave up is
+    ! reported here and stops the run, like any other failed call)
+    call check(les_gpu_sync(les_h), 'sync')
     call get3(LES_FIELD_U, u, 0, im + 1, -1, jm + 1, 0, km + 1)
     call get3(LES_FIELD_V, v, 0, im + 1, -1, jm + 1, 0, km + 1)
     call get3(LES_FIELD_W, w, 0, im + 1, -1, jm + 1, -1, km + 1)
